@@ -1,0 +1,203 @@
+"""CPU oracle for the guiding step -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package; it is the checker, never the thing measured or shipped.
+
+Two libraries sit behind it:
+  * oracle/_build/libnmg_oracle.so -- the scalar-templated C++ restatement
+    (nmg_oracle.hpp, oracle_capi.cpp), FP64 and reference-order FP32;
+  * oracle/_ref/libnmgref.so -- the reference's own mixture code compiled on
+    the host by oracle/build_ref.sh (only where the reference checkout exists;
+    used here to pin the restatement and to write tests/golden/).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+_ref = None
+
+
+class Opts(C.Structure):
+    _fields_ = [("kappa_poly", C.c_int), ("expm1_norm", C.c_int), ("kappa_softplus", C.c_int),
+                ("half_grad", C.c_int)]
+
+
+def opts(kappa_poly=1, expm1_norm=0, kappa_softplus=0, half_grad=0):
+    return Opts(kappa_poly, expm1_norm, kappa_softplus, half_grad)
+
+
+class Net(C.Structure):
+    _fields_ = [("input_mode", C.c_int), ("grid_hash", C.c_int), ("grid_levels", C.c_int),
+                ("grid_feats", C.c_int), ("grid_log2_T", C.c_int), ("grid_base_res", C.c_int),
+                ("grid_scale", C.c_float), ("grid_smoothstep", C.c_int), ("sh_degree", C.c_int),
+                ("oneblob_bins", C.c_int), ("width", C.c_int), ("n_hidden", C.c_int), ("n_out", C.c_int),
+                ("n_input", C.c_int), ("n_enc", C.c_int), ("n_enc_padded", C.c_int),
+                ("n_out_padded", C.c_int), ("n_mlp_params", C.c_long), ("n_grid_params", C.c_long),
+                ("n_params", C.c_long), ("n_entries", C.c_long), ("grid_offset", C.c_uint32 * 33)]
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.nmgo_num_threads.restype = C.c_int
+        L.nmgo_mixture_sample.argtypes = [C.c_int, P, C.c_int, C.c_int, C.c_long, P, P, C.POINTER(Opts), P, P, P]
+        L.nmgo_mixture_boundary_distance.argtypes = [P, C.c_int, C.c_int, C.c_long, P, P, C.POINTER(Opts), P]
+        L.nmgo_mixture_pdf.argtypes = [C.c_int, P, C.c_int, C.c_int, C.c_long, P, P, C.POINTER(Opts), P]
+        L.nmgo_mixture_loss_grad.argtypes = [C.c_int, C.c_int, P, C.c_int, C.c_int, C.c_long, P, C.c_int,
+                                             C.c_float, C.POINTER(Opts), P, P]
+        L.nmgo_mixture_loss_grad.restype = C.c_double
+        L.nmgo_net_init.argtypes = [C.POINTER(Net)]
+        L.nmgo_featurize.argtypes = [C.POINTER(Net), C.c_long, P, P, P, P, P, P]
+        L.nmgo_network_forward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P]
+        L.nmgo_network_backward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P, P]
+        L.nmgo_adam_ema.argtypes = [C.c_long, C.c_long, P, C.c_float, C.c_float, C.c_float, C.c_float,
+                                    C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P, P]
+        _lib = L
+    return _lib
+
+
+def num_threads():
+    return lib().nmgo_num_threads()
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f32(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+
+
+def mixture_sample(raw, K, u4, cos_normal=None, fp64=True, o=None):
+    raw, u4, cos_normal = _f32(raw), _f32(u4), _f32(cos_normal)
+    n = raw.shape[0]
+    d = np.zeros((n, 3), np.float64)
+    p = np.zeros(n, np.float64)
+    lb = np.zeros(n, np.int32)
+    o = o or opts()
+    lib().nmgo_mixture_sample(int(fp64), _p(raw), raw.shape[1], K, n, _p(u4), _p(cos_normal), C.byref(o),
+                              _p(d), _p(p), _p(lb))
+    return d, p, lb
+
+
+def boundary_distance(raw, K, u4, cos_normal=None, o=None):
+    raw, u4, cos_normal = _f32(raw), _f32(u4), _f32(cos_normal)
+    n = raw.shape[0]
+    out = np.zeros(n, np.float64)
+    o = o or opts()
+    lib().nmgo_mixture_boundary_distance(_p(raw), raw.shape[1], K, n, _p(u4), _p(cos_normal), C.byref(o), _p(out))
+    return out
+
+
+def mixture_pdf(raw, K, wi, cos_normal=None, fp64=True, o=None):
+    raw, wi, cos_normal = _f32(raw), _f32(wi), _f32(cos_normal)
+    n = raw.shape[0]
+    p = np.zeros(n, np.float64)
+    o = o or opts()
+    lib().nmgo_mixture_pdf(int(fp64), _p(raw), raw.shape[1], K, n, _p(wi), _p(cos_normal), C.byref(o), _p(p))
+    return p
+
+
+def mixture_loss_grad(raw, K, samples, loss_scale=128.0, selection=False, fp64=True, o=None):
+    """Returns (grad [n x stride] float64, loss [n] float64, FP64 loss sum)."""
+    raw, samples = _f32(raw), _f32(samples)
+    n = raw.shape[0]
+    g = np.zeros(raw.shape, np.float64)
+    loss = np.zeros(n, np.float64)
+    o = o or opts()
+    tot = lib().nmgo_mixture_loss_grad(int(fp64), int(selection), _p(raw), raw.shape[1], K, n, _p(samples),
+                                       samples.shape[1], float(loss_scale), C.byref(o), _p(g), _p(loss))
+    return g, loss, tot
+
+
+def make_net(**kw):
+    net = Net()
+    for k, v in kw.items():
+        setattr(net, k, v)
+    lib().nmgo_net_init(C.byref(net))
+    return net
+
+
+def featurize(net, pos, wo, nrm, rough, aabb):
+    pos, wo, nrm, rough, aabb = (_f32(x) for x in (pos, wo, nrm, rough, aabb))
+    n = pos.shape[0]
+    out = np.zeros((n, net.n_input), np.float32)
+    lib().nmgo_featurize(C.byref(net), n, _p(pos), _p(wo), _p(nrm), _p(rough), _p(aabb), _p(out))
+    return out
+
+
+def network_forward(net, params, inputs, want_enc=False):
+    params, inputs = _f32(params), _f32(inputs)
+    n = inputs.shape[0]
+    raw = np.zeros((n, net.n_out_padded), np.float64)
+    enc = np.zeros((n, net.n_enc_padded), np.float64) if want_enc else None
+    lib().nmgo_network_forward(C.byref(net), _p(params), n, _p(inputs), _p(raw), _p(enc))
+    return (raw, enc) if want_enc else raw
+
+
+def network_backward(net, params, inputs, draw, want_denc=False):
+    params, inputs = _f32(params), _f32(inputs)
+    draw = np.ascontiguousarray(draw, np.float64)
+    n = inputs.shape[0]
+    dparams = np.zeros(net.n_params, np.float64)
+    denc = np.zeros((n, net.n_enc_padded), np.float64) if want_denc else None
+    lib().nmgo_network_backward(C.byref(net), _p(params), n, _p(inputs), _p(draw), _p(dparams), _p(denc))
+    return (dparams, denc) if want_denc else dparams
+
+
+def adam_ema(grad, loss_scale, lr, beta1, beta2, eps, l2, ema_decay, step, w, m, v, psteps, ema, n_matrix):
+    """In-place Adam + EMA on float32 numpy arrays (psteps uint32)."""
+    grad = _f32(grad)
+    lib().nmgo_adam_ema(w.size, n_matrix, _p(grad), loss_scale, lr, beta1, beta2, eps, l2, ema_decay, step,
+                        _p(w), _p(m), _p(v), _p(psteps), _p(ema))
+
+
+# ------------------------------------------------------------ reference shim
+def ref_lib():
+    """The reference's own mixture code (None where it cannot be built)."""
+    global _ref
+    if _ref is None:
+        path = build_oracle.build_reference()
+        if path is None:
+            return None
+        L = C.CDLL(path)
+        P = C.c_void_p
+        L.ref_mixture_sample.argtypes = [P, C.c_int, C.c_long, P, P, P, P, P]
+        L.ref_mixture_pdf.argtypes = [P, C.c_int, C.c_long, P, P, P]
+        L.ref_loss_grad.argtypes = [P, C.c_int, C.c_long, P, C.c_float, P, P]
+        _ref = L
+    return _ref
+
+
+def ref_mixture_sample(raw, u4, cos_normal=None):
+    raw, u4, cos_normal = _f32(raw), _f32(u4), _f32(cos_normal)
+    n = raw.shape[0]
+    d = np.zeros((n, 3), np.float32)
+    p = np.zeros(n, np.float32)
+    lb = np.zeros(n, np.int32)
+    ref_lib().ref_mixture_sample(_p(raw), raw.shape[1], n, _p(u4), _p(cos_normal), _p(d), _p(p), _p(lb))
+    return d, p, lb
+
+
+def ref_mixture_pdf(raw, wi, cos_normal=None):
+    raw, wi, cos_normal = _f32(raw), _f32(wi), _f32(cos_normal)
+    n = raw.shape[0]
+    p = np.zeros(n, np.float32)
+    ref_lib().ref_mixture_pdf(_p(raw), raw.shape[1], n, _p(wi), _p(cos_normal), _p(p))
+    return p
+
+
+def ref_loss_grad(raw, samples, loss_scale=128.0):
+    raw, samples = _f32(raw), _f32(samples)
+    n = raw.shape[0]
+    g = np.zeros(raw.shape, np.float32)
+    loss = np.zeros(n, np.float32)
+    ref_lib().ref_loss_grad(_p(raw), raw.shape[1], n, _p(samples), float(loss_scale), _p(g), _p(loss))
+    return g, loss
