@@ -1,0 +1,341 @@
+"""GB300-native neural parametric mixture guiding step -- Python host binding.
+
+Thin ctypes layer over the C ABI of libnmg.so (declared in include/nmg.h).
+Tensors are torch CUDA tensors; only their device pointers cross the ABI.
+There is no CPU fallback: if the library is missing or was not built, every
+call raises.
+
+Mirrors the reference's guiding interface (src/render/guided/):
+  mixture_sample / mixture_pdf / mixture_loss_grad -- MixedSphericalGaussian-
+    Distribution's sample, pdf and the KL gradient kernel (distribution.h,
+    train.cu:69-172), on raw network outputs;
+  GuidingField -- the network-backed guide (GuidedPathTracer's inference and
+    training steps, integrator.cpp:627-701).
+"""
+import ctypes as C
+import os
+
+from . import build as _build
+
+_lib = None
+
+
+class NMGError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("nmg status %d: %s" % (status, msg))
+        self.status = status
+
+
+class MixtureOpts(C.Structure):
+    _fields_ = [("n_lobes", C.c_int), ("stride", C.c_int), ("kappa_softplus", C.c_int),
+                ("kappa_poly", C.c_int), ("selection", C.c_int)]
+
+
+def library_path():
+    return _build.LIB
+
+
+def lib():
+    """Load libnmg.so (building it first if its sources are newer)."""
+    global _lib
+    if _lib is None:
+        if os.environ.get("NMG_NO_BUILD") != "1":
+            _build.build()
+        if not os.path.exists(_build.LIB):
+            raise NMGError(-1, "libnmg.so not built at %s" % _build.LIB)
+        L = C.CDLL(_build.LIB)
+        P = C.c_void_p
+        L.nmg_status_string.restype = C.c_char_p
+        L.nmg_status_string.argtypes = [C.c_int]
+        L.nmg_last_error.restype = C.c_char_p
+        L.nmg_version.restype = C.c_int
+        L.nmg_mixture_sample.argtypes = [C.POINTER(MixtureOpts), P, P, P, C.c_int, P, P, P, P]
+        L.nmg_mixture_pdf.argtypes = [C.POINTER(MixtureOpts), P, P, P, C.c_int, P, P]
+        L.nmg_mixture_loss_workspace_bytes.restype = C.c_size_t
+        L.nmg_mixture_loss_workspace_bytes.argtypes = [C.c_int]
+        L.nmg_mixture_loss_grad.argtypes = [C.POINTER(MixtureOpts), P, P, C.c_int, C.c_int, C.c_float, P, P, P, P,
+                                            C.c_size_t, P]
+        for name in ("nmg_mixture_sample", "nmg_mixture_pdf", "nmg_mixture_loss_grad"):
+            getattr(L, name).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def check(status):
+    if status != 0:
+        L = lib()
+        raise NMGError(status, "%s (%s)" % (L.nmg_status_string(status).decode(), L.nmg_last_error().decode()))
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+def _stream(stream):
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return C.c_void_p(s.cuda_stream)
+
+
+def mixture_opts(n_lobes, stride, kappa_softplus=False, kappa_poly=True, selection=False):
+    return MixtureOpts(n_lobes, stride, int(kappa_softplus), int(kappa_poly), int(selection))
+
+
+def mixture_sample(raw, u4, n_lobes, cos_normal=None, kappa_softplus=False, want_lobe=True, stream=None):
+    """Sample one direction per query: returns (dir [n,3], pdf [n], lobe [n] or None)."""
+    import torch
+    n = raw.shape[0]
+    dev = raw.device
+    d = torch.empty((n, 3), device=dev, dtype=torch.float32)
+    p = torch.empty(n, device=dev, dtype=torch.float32)
+    lb = torch.empty(n, device=dev, dtype=torch.int32) if want_lobe else None
+    o = mixture_opts(n_lobes, raw.shape[1], kappa_softplus)
+    check(lib().nmg_mixture_sample(C.byref(o), _ptr(raw), _ptr(u4), _ptr(cos_normal), n, _ptr(d), _ptr(p), _ptr(lb),
+                                   _stream(stream)))
+    return d, p, lb
+
+
+def mixture_pdf(raw, wi, n_lobes, cos_normal=None, kappa_softplus=False, stream=None):
+    import torch
+    n = raw.shape[0]
+    p = torch.empty(n, device=raw.device, dtype=torch.float32)
+    o = mixture_opts(n_lobes, raw.shape[1], kappa_softplus)
+    check(lib().nmg_mixture_pdf(C.byref(o), _ptr(raw), _ptr(wi), _ptr(cos_normal), n, _ptr(p), _stream(stream)))
+    return p
+
+
+def mixture_loss_grad(raw, records, n_lobes, loss_scale=128.0, selection=False, kappa_softplus=False,
+                      kappa_poly=True, want_loss=True, stream=None):
+    """KL loss gradient w.r.t. raw outputs: returns (grad [n,stride], loss [n] or None, loss_sum [1] float64)."""
+    import torch
+    n = raw.shape[0]
+    dev = raw.device
+    g = torch.zeros_like(raw)
+    loss = torch.empty(n, device=dev, dtype=torch.float32) if want_loss else None
+    tot = torch.empty(1, device=dev, dtype=torch.float64)
+    L = lib()
+    wsb = L.nmg_mixture_loss_workspace_bytes(n)
+    ws = torch.empty(wsb, device=dev, dtype=torch.uint8)
+    o = mixture_opts(n_lobes, raw.shape[1], kappa_softplus, kappa_poly, selection)
+    check(L.nmg_mixture_loss_grad(C.byref(o), _ptr(raw), _ptr(records), records.shape[1], n, float(loss_scale),
+                                  _ptr(g), _ptr(loss), _ptr(tot), _ptr(ws), wsb, _stream(stream)))
+    return g, loss, tot
+
+
+# ---------------------------------------------------------------- guiding field
+PRESET_REFERENCE = 0
+PRESET_HASHGRID = 1
+PATH_FP32, PATH_BF16, PATH_FP16 = 0, 1, 2
+
+
+class Config(C.Structure):
+    _fields_ = [("n_lobes", C.c_int), ("selection", C.c_int), ("kappa_softplus", C.c_int), ("kappa_poly", C.c_int),
+                ("cosine_aware", C.c_int), ("input_mode", C.c_int), ("grid_hash", C.c_int),
+                ("grid_levels", C.c_int), ("grid_features", C.c_int), ("grid_log2_hashmap", C.c_int),
+                ("grid_base_resolution", C.c_int), ("grid_per_level_scale", C.c_float),
+                ("grid_smoothstep", C.c_int), ("sh_degree", C.c_int), ("oneblob_bins", C.c_int),
+                ("aabb", C.c_float * 6), ("width", C.c_int), ("hidden_layers", C.c_int), ("path", C.c_int),
+                ("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("l2_reg", C.c_float), ("ema_decay", C.c_float), ("use_ema", C.c_int), ("loss_scale", C.c_float),
+                ("seed", C.c_uint32)]
+
+
+class Info(C.Structure):
+    _fields_ = [("n_input", C.c_int), ("n_encoded", C.c_int), ("n_encoded_padded", C.c_int), ("n_output", C.c_int),
+                ("n_output_padded", C.c_int), ("n_mlp_params", C.c_int64), ("n_grid_params", C.c_int64),
+                ("n_params", C.c_int64), ("grid_entries", C.c_int64), ("record_floats", C.c_int)]
+
+
+class Shading(C.Structure):
+    _fields_ = [("pos", C.c_void_p), ("wo", C.c_void_p), ("normal", C.c_void_p), ("roughness", C.c_void_p)]
+
+
+class QueryOut(C.Structure):
+    _fields_ = [("dir", C.c_void_p), ("pdf", C.c_void_p), ("lobe", C.c_void_p), ("raw", C.c_void_p),
+                ("selection", C.c_void_p)]
+
+
+def _bind_field(L):
+    P = C.c_void_p
+    sig = {
+        "nmg_config_init": [C.POINTER(Config), C.c_int],
+        "nmg_config_info": [C.POINTER(Config), C.POINTER(Info)],
+        "nmg_create": [C.POINTER(Config), C.POINTER(P)],
+        "nmg_get_info": [P, C.POINTER(Info)],
+        "nmg_reserve": [P, C.c_int, C.c_int],
+        "nmg_set_params": [P, P, P],
+        "nmg_get_params": [P, C.c_int, P, P],
+        "nmg_get_gradients": [P, P, P],
+        "nmg_featurize": [P, C.POINTER(Shading), C.c_int, P, P],
+        "nmg_infer_raw": [P, P, C.c_int, C.c_int, P, P],
+        "nmg_query": [P, C.POINTER(Shading), P, P, C.c_int, C.POINTER(QueryOut), P],
+        "nmg_pdf": [P, C.POINTER(Shading), P, P, C.c_int, P, P],
+        "nmg_train_step": [P, P, P, P, C.c_int, P, P],
+        "nmg_network_vjp": [P, P, P, C.c_int, P, P, P],
+        "nmg_save": [P, C.c_char_p],
+        "nmg_load": [P, C.c_char_p],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = C.c_int
+    L.nmg_destroy.argtypes = [P]
+    L.nmg_destroy.restype = None
+    L.nmg_get_step.argtypes = [P]
+    L.nmg_get_step.restype = C.c_int
+
+
+def config(preset=PRESET_HASHGRID, **overrides):
+    cfg = Config()
+    L = lib()
+    if not hasattr(L, "_field_bound"):
+        _bind_field(L)
+        L._field_bound = True
+    check(L.nmg_config_init(C.byref(cfg), preset))
+    for k, v in overrides.items():
+        if k == "aabb":
+            for i in range(6):
+                cfg.aabb[i] = float(v[i])
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+class GuidingField:
+    """The network-backed guiding distribution (encoding -> MLP -> vMF mixture).
+
+    Mirrors GuidedPathTracer's guiding members (src/render/guided/
+    integrator.cpp): `query` is inferenceStep + the guided sample/pdf,
+    `pdf` the MIS pdf, `train_step` one batch of trainStep.
+    """
+
+    def __init__(self, cfg=None, max_queries=0, max_batch=0):
+        self.L = lib()
+        if not hasattr(self.L, "_field_bound"):
+            _bind_field(self.L)
+            self.L._field_bound = True
+        self.cfg = cfg if cfg is not None else config()
+        h = C.c_void_p()
+        check(self.L.nmg_create(C.byref(self.cfg), C.byref(h)))
+        self.h = h
+        self.info = Info()
+        check(self.L.nmg_get_info(self.h, C.byref(self.info)))
+        if max_queries or max_batch:
+            self.reserve(max_queries, max_batch)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nmg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, max_queries, max_batch):
+        check(self.L.nmg_reserve(self.h, int(max_queries), int(max_batch)))
+
+    @property
+    def n_params(self):
+        return int(self.info.n_params)
+
+    def get_params(self, which=0):
+        import torch
+        out = torch.empty(self.n_params, device="cuda", dtype=torch.float32)
+        check(self.L.nmg_get_params(self.h, which, _ptr(out), _stream(None)))
+        return out
+
+    def set_params(self, params):
+        check(self.L.nmg_set_params(self.h, _ptr(params), _stream(None)))
+
+    def get_gradients(self):
+        import torch
+        out = torch.empty(self.n_params, device="cuda", dtype=torch.float32)
+        check(self.L.nmg_get_gradients(self.h, _ptr(out), _stream(None)))
+        return out
+
+    @property
+    def step(self):
+        return self.L.nmg_get_step(self.h)
+
+    @staticmethod
+    def shading(pos, wo, normal, rough):
+        return Shading(pos.data_ptr(), wo.data_ptr(), normal.data_ptr(), rough.data_ptr())
+
+    def featurize(self, pos, wo, normal, rough, stream=None):
+        import torch
+        n = pos.shape[0]
+        x = torch.empty((n, self.info.n_input), device="cuda", dtype=torch.float32)
+        sh = self.shading(pos, wo, normal, rough)
+        check(self.L.nmg_featurize(self.h, C.byref(sh), n, _ptr(x), _stream(stream)))
+        return x
+
+    def infer_raw(self, x, which=1, stream=None):
+        import torch
+        n = x.shape[0]
+        raw = torch.empty((n, self.info.n_output_padded), device="cuda", dtype=torch.float32)
+        check(self.L.nmg_infer_raw(self.h, _ptr(x), n, which, _ptr(raw), _stream(stream)))
+        return raw
+
+    def query(self, pos, wo, normal, rough, u4, count=None, want_raw=False, outputs=None, stream=None):
+        """Returns dict(dir, pdf, lobe, raw?, selection?) for the first count (device int tensor) queries."""
+        import torch
+        n = pos.shape[0]
+        if outputs is None:
+            outputs = {
+                "dir": torch.empty((n, 3), device="cuda"),
+                "pdf": torch.empty(n, device="cuda"),
+                "lobe": torch.empty(n, device="cuda", dtype=torch.int32),
+            }
+            if want_raw:
+                outputs["raw"] = torch.empty((n, self.info.n_output_padded), device="cuda")
+            if self.cfg.selection:
+                outputs["selection"] = torch.empty(n, device="cuda")
+        o = QueryOut(*(outputs[k].data_ptr() if outputs.get(k) is not None else None
+                       for k in ("dir", "pdf", "lobe", "raw", "selection")))
+        sh = self.shading(pos, wo, normal, rough)
+        check(self.L.nmg_query(self.h, C.byref(sh), _ptr(u4), _ptr(count), n, C.byref(o), _stream(stream)))
+        return outputs
+
+    def pdf(self, pos, wo, normal, rough, wi, count=None, stream=None):
+        import torch
+        n = pos.shape[0]
+        p = torch.empty(n, device="cuda")
+        sh = self.shading(pos, wo, normal, rough)
+        check(self.L.nmg_pdf(self.h, C.byref(sh), _ptr(wi), _ptr(count), n, _ptr(p), _stream(stream)))
+        return p
+
+    def train_step(self, x, records, count=None, stats=None, stream=None):
+        """One optimiser step; returns a float64 device tensor [mean loss, grad norm]."""
+        import torch
+        if stats is None:
+            stats = torch.zeros(2, device="cuda", dtype=torch.float64)
+        check(self.L.nmg_train_step(self.h, _ptr(x), _ptr(records), _ptr(count), x.shape[0], _ptr(stats),
+                                    _stream(stream)))
+        return stats
+
+    def vjp(self, x, draw, dparams=None, stream=None):
+        import torch
+        n = x.shape[0]
+        raw = torch.empty((n, self.info.n_output_padded), device="cuda")
+        if dparams is None:
+            dparams = torch.zeros(self.n_params, device="cuda")
+        check(self.L.nmg_network_vjp(self.h, _ptr(x), _ptr(draw), n, _ptr(raw), _ptr(dparams), _stream(stream)))
+        return raw, dparams
+
+    def save(self, path):
+        check(self.L.nmg_save(self.h, path.encode()))
+
+    def load(self, path):
+        check(self.L.nmg_load(self.h, path.encode()))
+
+
+def oracle_net_spec(cfg):
+    """Keyword arguments for the oracle's network description of a config."""
+    return dict(input_mode=cfg.input_mode, grid_hash=cfg.grid_hash, grid_levels=cfg.grid_levels,
+                grid_feats=cfg.grid_features, grid_log2_T=cfg.grid_log2_hashmap,
+                grid_base_res=cfg.grid_base_resolution, grid_scale=cfg.grid_per_level_scale,
+                grid_smoothstep=cfg.grid_smoothstep, sh_degree=cfg.sh_degree, oneblob_bins=cfg.oneblob_bins,
+                width=cfg.width, n_hidden=cfg.hidden_layers, n_out=4 * cfg.n_lobes + (1 if cfg.selection else 0))

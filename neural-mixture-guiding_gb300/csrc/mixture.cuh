@@ -1,0 +1,334 @@
+// mixture.cuh -- FP32 device math of the K-lobe vMF mixture.
+//
+// Follows the reference's mixture (src/render/guided/distribution.h:13-202,
+// src/backend/src/util/vmf.h:12-75) with one thread per query and the lobes
+// held in registers. Mean directions are kept as unit vectors: the reference
+// stores them as spherical angles and converts back with sin/cos at every
+// evaluation (and through acos/atan2 after the cosine-lobe product,
+// distribution.h:54); the Cartesian form skips those round trips and is
+// closer to the exact value, not further from it.
+//
+// The FAST template flag selects hardware approximations (__expf, __sincosf,
+// __fdividef) for the fused reduced-precision path; FAST = false uses CUDA's
+// accurate expf/sincosf/log1pf for the FP32 path.
+#pragma once
+#include "common.cuh"
+
+namespace nmg {
+
+template <bool FAST> NMG_D float xexp(float x) { return FAST ? __expf(x) : expf(x); }
+template <bool FAST> NMG_D void xsincos(float x, float* s, float* c) {
+  if (FAST)
+    __sincosf(x, s, c);
+  else
+    sincosf(x, s, c);
+}
+template <bool FAST> NMG_D float xdiv(float a, float b) { return FAST ? __fdividef(a, b) : a / b; }
+
+// train.h:391-415 activations.
+NMG_D float act_exp_clamp(float x) { return fminf(fmaxf(x, -10.f), 15.f); }
+template <bool FAST> NMG_D float logistic(float x) { return xdiv<FAST>(1.f, 1.f + xexp<FAST>(-x)); }
+template <bool FAST> NMG_D float softplus(float x) { return FAST ? __logf(1.f + __expf(x)) : logf(1.f + expf(x)); }
+
+struct MixOpts {
+  int kappa_softplus;  // 0: kappa = exp(clamp(x)) (train.h:244); 1: log(1+e^x)
+  int kappa_poly;      // 1: distribution.h:165-166 polynomial for kappa < 1
+  int cosine;          // multiply by the cosine lobe before sampling/pdf
+};
+
+template <int K> struct Mix {
+  float lam[K];   // activated lambda (after any product)
+  float kap[K];   // concentration
+  f3 mu[K];       // unit mean direction
+  float w[K];     // normalised weight lambda/total
+  float total;
+};
+
+// vMF normaliser k / (2 pi (1 - e^{-2k})) (vmf.h:25-26); below M_EPSILON the
+// lobe is uniform (1/4pi).
+template <bool FAST> NMG_D float vmf_norm(float k) {
+  return k < NMG_EPS ? NMG_INV_4PI : xdiv<FAST>(k, NMG_TWO_PI * (1.f - xexp<FAST>(-2.f * k)));
+}
+
+// distribution.h:85-98: activation of one query's raw outputs. `raw` points
+// at 4K floats (lambda, kappa, theta, phi per lobe), 16-byte aligned.
+template <int K, bool FAST>
+NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
+  m.total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float4 r = reinterpret_cast<const float4*>(raw)[i];
+    m.lam[i] = xexp<FAST>(act_exp_clamp(r.x));
+    m.kap[i] = kappa_softplus ? softplus<FAST>(r.y) : xexp<FAST>(act_exp_clamp(r.y));
+    float th = NMG_PI * logistic<FAST>(r.z);
+    float ph = NMG_TWO_PI * logistic<FAST>(r.w);
+    float st, ct, sp, cp;
+    xsincos<FAST>(th, &st, &ct);
+    xsincos<FAST>(ph, &sp, &cp);
+    m.mu[i] = f3{st * cp, st * sp, ct};
+    m.total += m.lam[i];
+  }
+#pragma unroll
+  for (int i = 0; i < K; ++i) m.w[i] = m.lam[i] / m.total;
+}
+
+// distribution.h:39-64 + 184-195: product of every lobe with the cosine lobe
+// (kappa 2.18853) around `n` (already face-forwarded, any length), then
+// renormalisation with total clamped below at M_EPSILON.
+template <int K, bool FAST>
+NMG_D void mix_apply_cosine(Mix<K>& m, f3 n) {
+  const float kb = 2.18853f;
+  f3 mb = normalize3(n);
+  auto pnorm = [](float k) {
+    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, 1.f - xexp<FAST>(-2.f * k));
+  };
+  const float nb = pnorm(kb);
+  m.total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    f3 ma = m.mu[i];
+    float ka = m.kap[i];
+    f3 nm = add3(scale3(ma, ka), scale3(mb, kb));
+    float nk = sqrtf(dot3(nm, nm));
+    if (nk >= 1e-3f) {
+      nm = f3{nm.x / nk, nm.y / nk, nm.z / nk};
+    } else {
+      nk = 0.f;
+      nm = ma;
+    }
+    float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
+    float s = xdiv<FAST>(pnorm(ka) * nb, pnorm(nk)) * e;
+    m.lam[i] = s * m.lam[i];
+    m.kap[i] = nk;
+    m.mu[i] = nm;
+    m.total += m.lam[i];
+  }
+  m.total = fmaxf(m.total, NMG_EPS);
+#pragma unroll
+  for (int i = 0; i < K; ++i) m.w[i] = m.lam[i] / m.total;
+}
+
+// distribution.h:132-140: lobe selection by sequential CDF subtraction,
+// falling back to lobe 0.
+template <int K> NMG_D int mix_select(const Mix<K>& m, float u) {
+  int sel = -1;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    if (sel < 0) {
+      if (u < m.w[i])
+        sel = i;
+      else
+        u -= m.w[i];
+    }
+  }
+  return sel < 0 ? 0 : sel;
+}
+
+// vmf.h:48-71: sample lobe `sel` with two uniforms, rotated by the frame of
+// its mean (raytracing.h:35-49, getPerpendicular math_utils.h:141-151).
+template <int K, bool FAST>
+NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
+  float k = 0.f;
+  f3 mu = m.mu[0];
+#pragma unroll
+  for (int i = 0; i < K; ++i)
+    if (i == sel) {
+      k = m.kap[i];
+      mu = m.mu[i];
+    }
+  f3 loc;
+  float ph = NMG_TWO_PI * u1;
+  float sp, cp;
+  if (k < NMG_EPS) {  // render/sampling.h:32-37
+    float z = 1.f - 2.f * u0;
+    float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+    xsincos<FAST>(ph, &sp, &cp);
+    return f3{r * cp, r * sp, z};
+  }
+  float ct = 1.f + log1pf(-u0 + xexp<FAST>(-2.f * k) * u0) / k;
+  float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+  xsincos<FAST>(ph, &sp, &cp);
+  loc = f3{cp * st, sp * st, ct};
+  // Frame(mu): T = normalize(mu x e), e the branchless axis pick; B = normalize(mu x T)
+  float ax = fabsf(mu.x), ay = fabsf(mu.y), az = fabsf(mu.z);
+  unsigned xm = ((ax - ay) < 0.f) & ((ax - az) < 0.f);
+  unsigned ym = (1u ^ xm) & ((ay - az) < 0.f);
+  unsigned zm = 1u ^ (xm | ym);
+  f3 t = normalize3(cross3(mu, f3{float(xm), float(ym), float(zm)}));
+  f3 b = normalize3(cross3(mu, t));
+  return f3{t.x * loc.x + b.x * loc.y + mu.x * loc.z, t.y * loc.x + b.y * loc.y + mu.y * loc.z,
+            t.z * loc.x + b.z * loc.y + mu.z * loc.z};
+}
+
+// distribution.h:113-119 with vmf.h:22-27: mixture pdf at unit direction wi.
+template <int K, bool FAST>
+NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
+  float p = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float k = m.kap[i];
+    float c = dot3(wi, m.mu[i]);
+    float v = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, c - 1.f)) * vmf_norm<FAST>(k);
+    p += m.w[i] * v;
+  }
+  return p;
+}
+
+// Per-sample KL loss and gradient with respect to the raw outputs
+// (train.cu:69-124, distribution.h:144-181), FP32.
+//   raw: 4K raw outputs (16-byte aligned); rec: GuidedOutput {theta, phi,
+//   L_r, L_g, L_b, wiPdf}; scale = loss_scale / batch size.
+// dF/dlambda uses the O(K) form (vmf_s - q)/total, algebraically equal to
+// the reference's O(K^2) sum. NaN/Inf gradients become 0 and gradients are
+// clamped above at 150 (train.cu:109-123). Returns the per-sample loss.
+template <int K, bool FAST>
+NMG_D float mix_kl_loss_grad(const float* raw, const float* rec, float scale, const MixOpts& o, float* grad) {
+  float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
+  float total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float4 r = reinterpret_cast<const float4*>(raw)[i];
+    lam[i] = xexp<FAST>(act_exp_clamp(r.x));
+    if (o.kappa_softplus) {
+      float e = xexp<FAST>(r.y);
+      kap[i] = FAST ? __logf(1.f + e) : logf(1.f + e);
+      dkap[i] = xdiv<FAST>(e, e + 1.f);
+    } else {
+      kap[i] = xexp<FAST>(act_exp_clamp(r.y));
+      dkap[i] = kap[i];  // train.h:410: derivative ignores the clamp
+    }
+    sgt[i] = logistic<FAST>(r.z);
+    sgp[i] = logistic<FAST>(r.w);
+    xsincos<FAST>(NMG_PI * sgt[i], &sth[i], &cth[i]);
+    xsincos<FAST>(NMG_TWO_PI * sgp[i], &sph[i], &cph[i]);
+    total += lam[i];
+  }
+  float swt, cwt, swp, cwp;
+  xsincos<FAST>(rec[0], &swt, &cwt);
+  xsincos<FAST>(rec[1], &swp, &cwp);
+  const f3 wi{swt * cwp, swt * swp, cwt};
+  float vmf[K];
+  float q = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float k = kap[i];
+    float c = wi.x * sth[i] * cph[i] + wi.y * sth[i] * sph[i] + wi.z * cth[i];
+    vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, c - 1.f)) * vmf_norm<FAST>(k);
+    q += (lam[i] / total) * vmf[i];
+  }
+  const float Li = (rec[2] + (rec[3] + rec[4])) / 3.f;
+  const float wp = rec[5] + NMG_EPS;
+  const float guide = q + NMG_EPS;
+  const float prefix = -Li / wp / guide * scale;
+  const float loss = -Li / wp * logf(guide);
+  const float inv_total = 1.f / total;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float k = kap[i];
+    float wv = (lam[i] * inv_total) * vmf[i];
+    float ik;
+    if (o.kappa_poly && k < 1.f) {
+      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+    } else if (!o.kappa_poly && k < 1e-2f) {
+      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+    } else {
+      float e = xexp<FAST>(-2.f * k);
+      ik = 1.f / k - (1.f + e) / (1.f - e);
+    }
+    float c = wi.x * sth[i] * cph[i] + wi.y * sth[i] * sph[i] + wi.z * cth[i];
+    float dl = (vmf[i] - q) * inv_total;
+    float dk = wv * (c + ik);
+    float dt = wv * k * (cth[i] * (wi.x * cph[i] + wi.y * sph[i]) - wi.z * sth[i]);
+    float dp = wv * k * (wi.y * cph[i] - wi.x * sph[i]) * sth[i];
+    float g0 = prefix * dl * lam[i];
+    float g1 = prefix * dk * dkap[i];
+    float g2 = prefix * dt * NMG_PI * (sgt[i] * (1.f - sgt[i]));
+    float g3 = prefix * dp * NMG_TWO_PI * (sgp[i] * (1.f - sgp[i]));
+    g0 = isfinite(g0) ? fminf(g0, 150.f) : 0.f;
+    g1 = isfinite(g1) ? fminf(g1, 150.f) : 0.f;
+    g2 = isfinite(g2) ? fminf(g2, 150.f) : 0.f;
+    g3 = isfinite(g3) ? fminf(g3, 150.f) : 0.f;
+    grad[4 * i + 0] = g0;
+    grad[4 * i + 1] = g1;
+    grad[4 * i + 2] = g2;
+    grad[4 * i + 3] = g3;
+  }
+  return loss;
+}
+
+// train.cu:126-172: the learned-selection variant. raw[4K] is the selection
+// logit; rec[6] the BSDF pdf of the direction. No NaN/clamp post-pass
+// (the reference has none for this variant). grad has 4K+1 entries.
+template <int K, bool FAST>
+NMG_D float mix_kl_loss_grad_selection(const float* raw, const float* rec, float scale, const MixOpts& o,
+                                       float* grad) {
+  float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
+  float total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float4 r = reinterpret_cast<const float4*>(raw)[i];
+    lam[i] = xexp<FAST>(act_exp_clamp(r.x));
+    if (o.kappa_softplus) {
+      float e = xexp<FAST>(r.y);
+      kap[i] = FAST ? __logf(1.f + e) : logf(1.f + e);
+      dkap[i] = xdiv<FAST>(e, e + 1.f);
+    } else {
+      kap[i] = xexp<FAST>(act_exp_clamp(r.y));
+      dkap[i] = kap[i];
+    }
+    sgt[i] = logistic<FAST>(r.z);
+    sgp[i] = logistic<FAST>(r.w);
+    xsincos<FAST>(NMG_PI * sgt[i], &sth[i], &cth[i]);
+    xsincos<FAST>(NMG_TWO_PI * sgp[i], &sph[i], &cph[i]);
+    total += lam[i];
+  }
+  const float xs = raw[4 * K];
+  const float sel = logistic<FAST>(xs);
+  float swt, cwt, swp, cwp;
+  xsincos<FAST>(rec[0], &swt, &cwt);
+  xsincos<FAST>(rec[1], &swp, &cwp);
+  const f3 wi{swt * cwp, swt * swp, cwt};
+  float vmf[K];
+  float q = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float k = kap[i];
+    float c = wi.x * sth[i] * cph[i] + wi.y * sth[i] * sph[i] + wi.z * cth[i];
+    vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, c - 1.f)) * vmf_norm<FAST>(k);
+    q += (lam[i] / total) * vmf[i];
+  }
+  const float Li = (rec[2] + (rec[3] + rec[4])) / 3.f;
+  const float bsdf = rec[6];
+  const float guide = q + NMG_EPS;
+  const float wp = sel * guide + (1.f - sel) * bsdf;
+  const float loss = -Li / wp * logf(wp);
+  const float prefix = -Li / wp / wp * scale;
+  const float inv_total = 1.f / total;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    float k = kap[i];
+    float wv = (lam[i] * inv_total) * vmf[i];
+    float ik;
+    if (o.kappa_poly && k < 1.f) {
+      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+    } else if (!o.kappa_poly && k < 1e-2f) {
+      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+    } else {
+      float e = xexp<FAST>(-2.f * k);
+      ik = 1.f / k - (1.f + e) / (1.f - e);
+    }
+    float c = wi.x * sth[i] * cph[i] + wi.y * sth[i] * sph[i] + wi.z * cth[i];
+    float dl = (vmf[i] - q) * inv_total * sel;
+    float dk = wv * (c + ik) * sel;
+    float dt = wv * k * (cth[i] * (wi.x * cph[i] + wi.y * sph[i]) - wi.z * sth[i]) * sel;
+    float dp = wv * k * (wi.y * cph[i] - wi.x * sph[i]) * sth[i] * sel;
+    grad[4 * i + 0] = prefix * dl * lam[i];
+    grad[4 * i + 1] = prefix * dk * dkap[i];
+    grad[4 * i + 2] = prefix * dt * NMG_PI * (sgt[i] * (1.f - sgt[i]));
+    grad[4 * i + 3] = prefix * dp * NMG_TWO_PI * (sgp[i] * (1.f - sgp[i]));
+  }
+  grad[4 * K] = 0.01f * prefix * (q - bsdf) * (sel * (1.f - sel));
+  return loss;
+}
+
+}  // namespace nmg

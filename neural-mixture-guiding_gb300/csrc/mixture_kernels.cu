@@ -1,0 +1,256 @@
+// mixture_kernels.cu -- FP32 mixture kernels on raw network outputs and their
+// C-ABI entry points (nmg_mixture_*).
+//
+// One thread per query, lobes in registers, grid-stride loops over a grid of
+// a few waves of the 152 SMs. Each query reads its raw row with 128-bit
+// loads (K float4) and its uniforms as one float4.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include "api_common.cuh"
+#include "mixture.cuh"
+
+namespace nmg {
+
+static thread_local char g_err[512] = "";
+
+nmg_status set_error(nmg_status st, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return st;
+}
+
+constexpr int kThreads = 128;
+
+static int grid_for(long n) {
+  long blocks = (n + kThreads - 1) / kThreads;
+  long cap = 152L * 16;  // 16 resident 128-thread blocks per SM
+  return int(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
+}
+
+template <int K, bool FAST>
+__global__ void __launch_bounds__(kThreads) k_mixture_sample(const float* __restrict__ raw, int stride,
+                                                             const float* __restrict__ u4,
+                                                             const float* __restrict__ cosn, int n,
+                                                             int kappa_softplus, float* __restrict__ dir,
+                                                             float* __restrict__ pdf, int* __restrict__ lobe) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
+    Mix<K> m;
+    mix_activate<K, FAST>(m, raw + q * stride, kappa_softplus);
+    if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
+    float4 u = reinterpret_cast<const float4*>(u4)[q];
+    int sel = mix_select<K>(m, u.y);
+    f3 d = mix_sample_lobe<K, FAST>(m, sel, u.z, u.w);
+    store3(dir, q, d);
+    pdf[q] = mix_pdf<K, FAST>(m, d);
+    if (lobe) lobe[q] = sel;
+  }
+}
+
+template <int K, bool FAST>
+__global__ void __launch_bounds__(kThreads) k_mixture_pdf(const float* __restrict__ raw, int stride,
+                                                          const float* __restrict__ wi,
+                                                          const float* __restrict__ cosn, int n,
+                                                          int kappa_softplus, float* __restrict__ pdf) {
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
+    Mix<K> m;
+    mix_activate<K, FAST>(m, raw + q * stride, kappa_softplus);
+    if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
+    pdf[q] = mix_pdf<K, FAST>(m, load3(wi, q));
+  }
+}
+
+// Sums `v` over the block in a fixed order; the result is valid in thread 0.
+__device__ __forceinline__ double block_sum_fixed(double v) {
+  __shared__ double s[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) s[wid] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) r += s[w];
+  __syncthreads();
+  return r;
+}
+
+template <int K, bool SEL>
+__global__ void __launch_bounds__(kThreads) k_mixture_loss_grad(const float* __restrict__ raw, int stride,
+                                                                const float* __restrict__ rec, int rstride,
+                                                                int n, float scale, MixOpts o,
+                                                                float* __restrict__ grad,
+                                                                float* __restrict__ loss,
+                                                                double* __restrict__ partials) {
+  double acc = 0.0;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
+    float r[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
+    float g[4 * K + 1];
+    float l = SEL ? mix_kl_loss_grad_selection<K, false>(raw + q * stride, r, scale, o, g)
+                  : mix_kl_loss_grad<K, false>(raw + q * stride, r, scale, o, g);
+    float4* gr = reinterpret_cast<float4*>(grad + q * stride);
+#pragma unroll
+    for (int i = 0; i < K; ++i) gr[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
+    if (SEL) grad[q * stride + 4 * K] = g[4 * K];
+    if (loss) loss[q] = l;
+    acc += double(l);
+  }
+  double s = block_sum_fixed(acc);
+  if (threadIdx.x == 0 && partials) partials[blockIdx.x] = s;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partials, int m, double* __restrict__ out) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) v += partials[i];
+  double s = block_sum_fixed(v);
+  if (threadIdx.x == 0) *out = s;
+}
+
+template <int K>
+static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, const float* u4, const float* cosn,
+                                int n, float* dir, float* pdf, int* lobe, cudaStream_t st) {
+  k_mixture_sample<K, false><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
+                                                               dir, pdf, lobe);
+  return check_launch("nmg_mixture_sample");
+}
+
+template <int K>
+static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const float* wi, const float* cosn, int n,
+                             float* pdf, cudaStream_t st) {
+  k_mixture_pdf<K, false><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
+  return check_launch("nmg_mixture_pdf");
+}
+
+template <int K>
+static nmg_status launch_loss(const nmg_mixture_opts* o, const float* raw, const float* rec, int rstride, int n,
+                              float loss_scale, float* grad, float* loss, double* loss_sum, double* partials,
+                              cudaStream_t st) {
+  MixOpts mo{o->kappa_softplus, o->kappa_poly, 0};
+  const int blocks = grid_for(n);
+  const float scale = loss_scale / float(n);
+  if (o->selection)
+    k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
+                                                              loss_sum ? partials : nullptr);
+  else
+    k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
+                                                               loss_sum ? partials : nullptr);
+  nmg_status s = check_launch("nmg_mixture_loss_grad");
+  if (s != NMG_OK || !loss_sum) return s;
+  k_sum_partials<<<1, 256, 0, st>>>(partials, blocks, loss_sum);
+  return check_launch("nmg_mixture_loss_grad (sum)");
+}
+
+static nmg_status check_opts(const nmg_mixture_opts* o) {
+  NMG_REQUIRE(o != nullptr, "opts is NULL");
+  NMG_REQUIRE(o->n_lobes == 4 || o->n_lobes == 7 || o->n_lobes == 8 || o->n_lobes == 16,
+              "n_lobes=%d: compiled lobe counts are 4, 7, 8 and 16", o->n_lobes);
+  NMG_REQUIRE(o->stride % 4 == 0, "stride=%d must be a multiple of 4", o->stride);
+  NMG_REQUIRE(o->stride >= 4 * o->n_lobes + (o->selection ? 1 : 0), "stride=%d too small for %d lobes%s",
+              o->stride, o->n_lobes, o->selection ? " + selection" : "");
+  return NMG_OK;
+}
+
+}  // namespace nmg
+
+using namespace nmg;
+
+extern "C" {
+
+const char* nmg_status_string(int s) {
+  switch (s) {
+    case NMG_OK: return "ok";
+    case NMG_ERR_INVALID_ARG: return "invalid argument";
+    case NMG_ERR_OOM: return "out of device memory";
+    case NMG_ERR_CUDA: return "CUDA error";
+    case NMG_ERR_NUMERIC: return "non-finite values";
+    case NMG_ERR_TIMEOUT: return "device wait timed out";
+    case NMG_ERR_UNSUPPORTED: return "unsupported configuration";
+    case NMG_ERR_CAPACITY: return "size above reserved capacity";
+    default: return "unknown status";
+  }
+}
+
+const char* nmg_last_error(void) { return g_err; }
+
+int nmg_version(void) { return 100; }
+
+nmg_status nmg_mixture_sample(const nmg_mixture_opts* opts, const float* raw, const float* u4, const float* cos_normal,
+                              int n, float* dir, float* pdf, int* lobe, nmg_stream stream) {
+  nmg_status s = check_opts(opts);
+  if (s != NMG_OK) return s;
+  NMG_REQUIRE(n >= 0, "n=%d < 0", n);
+  if (n == 0) return NMG_OK;
+  NMG_REQUIRE(raw && u4 && dir && pdf, "raw, u4, dir and pdf must be non-NULL");
+  NMG_REQUIRE(aligned16(raw) && aligned16(u4), "raw and u4 must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+#define CALL(K) launch_sample<K>(opts, raw, u4, cos_normal, n, dir, pdf, lobe, st)
+  switch (opts->n_lobes) {
+    case 4: return CALL(4);
+    case 7: return CALL(7);
+    case 8: return CALL(8);
+    case 16: return CALL(16);
+  }
+#undef CALL
+  return NMG_ERR_UNSUPPORTED;
+}
+
+nmg_status nmg_mixture_pdf(const nmg_mixture_opts* opts, const float* raw, const float* wi, const float* cos_normal,
+                           int n, float* pdf, nmg_stream stream) {
+  nmg_status s = check_opts(opts);
+  if (s != NMG_OK) return s;
+  NMG_REQUIRE(n >= 0, "n=%d < 0", n);
+  if (n == 0) return NMG_OK;
+  NMG_REQUIRE(raw && wi && pdf, "raw, wi and pdf must be non-NULL");
+  NMG_REQUIRE(aligned16(raw), "raw must be 16-byte aligned");
+  cudaStream_t st = (cudaStream_t)stream;
+#define CALL(K) launch_pdf<K>(opts, raw, wi, cos_normal, n, pdf, st)
+  switch (opts->n_lobes) {
+    case 4: return CALL(4);
+    case 7: return CALL(7);
+    case 8: return CALL(8);
+    case 16: return CALL(16);
+  }
+#undef CALL
+  return NMG_ERR_UNSUPPORTED;
+}
+
+size_t nmg_mixture_loss_workspace_bytes(int n) { return sizeof(double) * size_t(grid_for(n < 1 ? 1 : n)); }
+
+nmg_status nmg_mixture_loss_grad(const nmg_mixture_opts* opts, const float* raw, const float* record,
+                                 int record_stride, int n, float loss_scale, float* grad, float* loss,
+                                 double* loss_sum, void* workspace, size_t workspace_bytes, nmg_stream stream) {
+  nmg_status s = check_opts(opts);
+  if (s != NMG_OK) return s;
+  NMG_REQUIRE(n >= 0, "n=%d < 0", n);
+  NMG_REQUIRE(record_stride >= (opts->selection ? 7 : 6) && record_stride <= 8,
+              "record_stride=%d: GuidedOutput rows have 6 floats (7 with selection), at most 8", record_stride);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    if (loss_sum) NMG_CUDA_TRY(cudaMemsetAsync(loss_sum, 0, sizeof(double), st));
+    return NMG_OK;
+  }
+  NMG_REQUIRE(raw && record && grad, "raw, record and grad must be non-NULL");
+  NMG_REQUIRE(aligned16(raw) && aligned16(grad), "raw and grad must be 16-byte aligned");
+  if (loss_sum) {
+    NMG_REQUIRE(workspace != nullptr, "loss_sum needs a workspace");
+    NMG_REQUIRE(workspace_bytes >= nmg_mixture_loss_workspace_bytes(n), "workspace_bytes=%zu < %zu", workspace_bytes,
+                nmg_mixture_loss_workspace_bytes(n));
+  }
+#define CALL(K) launch_loss<K>(opts, raw, record, record_stride, n, loss_scale, grad, loss, loss_sum, \
+                               (double*)workspace, st)
+  switch (opts->n_lobes) {
+    case 4: return CALL(4);
+    case 7: return CALL(7);
+    case 8: return CALL(8);
+    case 16: return CALL(16);
+  }
+#undef CALL
+  return NMG_ERR_UNSUPPORTED;
+}
+
+}  // extern "C"

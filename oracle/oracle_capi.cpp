@@ -346,13 +346,53 @@ extern "C" void nmgo_network_forward(const nmgo_net* net, const float* params, l
   }
 }
 
+// grid_backward with OpenMP atomic accumulation (same weights as the forward).
+static void grid_backward_atomic(const GridSpec& g, const float pos[3], const double* dfeat, double* grad) {
+  float l2s = std::log2(g.per_level_scale);
+  for (int l = 0; l < g.levels; ++l) {
+    float scale = grid_scale(uint32_t(l), l2s, uint32_t(g.base_res));
+    uint32_t res = grid_resolution(scale);
+    uint32_t T = g.offset[l + 1] - g.offset[l];
+    double w[3];
+    uint32_t pg[3];
+    for (int d = 0; d < 3; ++d) {
+      float p = pos[d] * scale + 0.5f;
+      float fl = floorf(p);
+      pg[d] = uint32_t(int(fl));
+      double f = double(p - fl);
+      w[d] = g.smoothstep ? f * f * (3.0 - 2.0 * f) : f;
+    }
+    for (int c = 0; c < 8; ++c) {
+      double wt = 1;
+      uint32_t lp[3];
+      for (int d = 0; d < 3; ++d) {
+        if ((c & (1 << d)) == 0) {
+          wt *= 1.0 - w[d];
+          lp[d] = pg[d];
+        } else {
+          wt *= w[d];
+          lp[d] = pg[d] + 1;
+        }
+      }
+      uint32_t idx = (g.offset[l] + grid_index(g.hash, T, res, lp)) * uint32_t(g.feats);
+      for (int f = 0; f < g.feats; ++f) {
+#pragma omp atomic
+        grad[idx + f] += wt * dfeat[l * g.feats + f];
+      }
+    }
+  }
+}
+
 // Network backward: dL/draw [n x n_out_padded] -> dL/dparams (accumulated,
 // FP64, same layout as params) and optionally dL/dencoded [n x n_enc_padded].
 extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, long n, const float* inputs,
                            const double* draw, double* dparams, double* denc_out) {
   GridSpec g = grid_of(net);
   int nt = nmgo_num_threads();
-  std::vector<std::vector<double>> part(nt, std::vector<double>(net->n_params, 0.0));
+  // MLP gradient: per-thread partials (small); grid gradient: atomic adds
+  // straight into dparams (the table is large and sparsely touched).
+  std::vector<std::vector<double>> part(nt, std::vector<double>(net->n_mlp_params, 0.0));
+  double* dgrid = dparams + net->n_mlp_params;
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < n; ++i) {
 #ifdef _OPENMP
@@ -400,10 +440,10 @@ extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, 
     }
     if (denc_out)
       for (int k = 0; k < net->n_enc_padded; ++k) denc_out[i * net->n_enc_padded + k] = dn[k];
-    grid_backward<double>(g, x, dn, acc.data() + net->n_mlp_params);
+    grid_backward_atomic(g, x, dn, dgrid);
   }
   for (int t = 0; t < nt; ++t)
-    for (long k = 0; k < net->n_params; ++k) dparams[k] += part[t][k];
+    for (long k = 0; k < net->n_mlp_params; ++k) dparams[k] += part[t][k];
 }
 
 // Adam (adam.h:47-119) followed by EMA (ema.h:62-75,102-145) over all params.
