@@ -1,0 +1,396 @@
+"""Benchmark of the guiding step (one JSON line on rank 0).
+
+Workload ("full guiding step", hash-grid network): each step is
+  * one guided query pass over a 1920x1080 wavefront (2,073,600 queries:
+    featurise -> hash-grid/SH/one-blob encode -> 80-64-64-64-48 MLP -> 8-lobe
+    vMF mixture with cosine lobe -> sample + pdf), and
+  * one training step on 2^18 records (forward, KL loss + adjoint, backward
+    through MLP and grid, Adam + EMA over 12.6 M parameters).
+Inputs are seeded synthetic data with the shapes and distributions of that
+workload (neural-mixture-guiding_gb300/synth.py), resident in HBM.
+
+value = guided queries/s of the measured path (default: fused BF16 on
+tcgen05); the same line carries train samples/s and the plain FP32 path's
+numbers measured in the same run. L2 is flushed (a 256 MiB write) before
+every timed step; each step is timed with CUDA events on the launching
+stream, excluding the flush.
+
+--impl reference times the reference algorithm on the host cores instead:
+the CPU restatement of the reference's guiding step (oracle/), OpenMP over
+all host threads, on a bounded sample of the same workload.
+"""
+import argparse
+import ctypes
+import importlib
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+PKG = "neural-mixture-guiding_gb300"
+
+N_QUERIES = 1920 * 1080
+N_TRAIN = 1 << 18
+FLOP_PER_QUERY = 2 * (80 * 64 + 64 * 64 + 64 * 64 + 64 * 48)  # 32,768 executed (padded) MLP FLOP
+BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, rough, u4 in; dir, pdf, lobe, sel out
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self):
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                          "--query-gpu=" + q, "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        dist.init_process_group("nccl")
+    return ws, rank
+
+
+def barrier_max(x, ws):
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def make_inputs(synth, torch, seed=7272):
+    q = synth.wavefront(N_QUERIES, seed=seed)
+    field = synth.TrainField(seed=seed)
+    x, rec = synth.train_batch(field, N_TRAIN, seed=seed + 1, input_mode=1, selection=True)
+    return q, x, rec
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    nmg = importlib.import_module(PKG)
+    synth = importlib.import_module(PKG + ".synth")
+    ws, rank = dist_setup()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    q, x, rec = make_inputs(synth, torch, seed=7272 + rank)
+    dq = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items()}
+    dx, drec = torch.from_numpy(x).cuda(), torch.from_numpy(rec).cuda()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    path = {"bf16": nmg.PATH_BF16, "fp16": nmg.PATH_FP16, "fp32": nmg.PATH_FP32}[args.path]
+
+    def measure(path_id, steps, warmup, clocks=None):
+        f = nmg.GuidingField(nmg.config(nmg.PRESET_HASHGRID, path=path_id), max_queries=N_QUERIES, max_batch=N_TRAIN)
+        out = {"dir": torch.empty((N_QUERIES, 3), device="cuda"), "pdf": torch.empty(N_QUERIES, device="cuda"),
+               "lobe": torch.empty(N_QUERIES, device="cuda", dtype=torch.int32),
+               "selection": torch.empty(N_QUERIES, device="cuda")}
+        stats = torch.zeros(2, device="cuda", dtype=torch.float64)
+        st = torch.cuda.current_stream()
+        ev = [(torch.cuda.Event(True), torch.cuda.Event(True), torch.cuda.Event(True)) for _ in range(steps)]
+        for _ in range(warmup):
+            f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
+            f.train_step(dx, drec, stats=stats)
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+        if clocks:
+            clocks.start()
+        t0 = time.perf_counter()
+        for i in range(steps):
+            flush.fill_(i & 0xff)
+            a, b, c = ev[i]
+            a.record(st)
+            f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
+            b.record(st)
+            f.train_step(dx, drec, stats=stats)
+            c.record(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        if ws > 1:
+            torch.distributed.barrier()
+        cl = clocks.stop() if clocks else None
+        tq = sum(a.elapsed_time(b) for a, b, _ in ev) / 1e3
+        tt = sum(b.elapsed_time(c) for _, b, c in ev) / 1e3
+        loss = stats.cpu().numpy().tolist()
+        # one more query with the raw outputs kept, for the kernel-only timing of the query kernel
+        f.L.nmg_check_errors.argtypes = [ctypes.c_void_p]
+        nmg.check(f.L.nmg_check_errors(f.h))
+        res = {"t_query": barrier_max(tq, ws), "t_train": barrier_max(tt, ws), "wall": wall, "clocks": cl,
+               "loss": loss, "field": f, "out": out}
+        return res
+
+    ours = measure(path, args.steps, args.warmup, Clocks())
+    plain = measure(nmg.PATH_FP32, max(1, min(args.steps, 3)), 1) if path != nmg.PATH_FP32 else ours
+
+    # end to end through the public API: pinned host inputs in, host results out, every step
+    f = ours["field"]
+    hq = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in q.items()}
+    hx, hrec = torch.from_numpy(x).pin_memory(), torch.from_numpy(rec).pin_memory()
+    hout_dir = torch.empty((N_QUERIES, 3)).pin_memory()
+    hout_pdf = torch.empty(N_QUERIES).pin_memory()
+    hstats = torch.empty(2, dtype=torch.float64).pin_memory()
+    h2d = sum(t.numel() * t.element_size() for k, t in hq.items() if k != "aabb") + hx.numel() * 4 + hrec.numel() * 4
+    d2h = hout_dir.numel() * 4 + hout_pdf.numel() * 4 + 16
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
+    e2e_steps = max(1, min(args.steps, 5))
+    e0.record()
+    for _ in range(e2e_steps):
+        for k in ("pos", "wo", "normal", "rough", "u4"):
+            dq[k].copy_(hq[k], non_blocking=True)
+        dx.copy_(hx, non_blocking=True)
+        drec.copy_(hrec, non_blocking=True)
+        o = f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=ours["out"])
+        s = f.train_step(dx, drec)
+        hout_dir.copy_(o["dir"], non_blocking=True)
+        hout_pdf.copy_(o["pdf"], non_blocking=True)
+        hstats.copy_(s, non_blocking=True)
+    e1.record()
+    torch.cuda.synchronize()
+    t_e2e = barrier_max(e0.elapsed_time(e1) / 1e3, ws)
+
+    # kernel-only timing of the fused query kernel (dominant kernel) on its own stream
+    st = torch.cuda.current_stream()
+    kk = []
+    for i in range(5):
+        flush.fill_(i)
+        a, b = torch.cuda.Event(True), torch.cuda.Event(True)
+        a.record(st)
+        f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=ours["out"])
+        b.record(st)
+        kk.append((a, b))
+    torch.cuda.synchronize()
+    t_kernel = sorted(a.elapsed_time(b) for a, b in kk)[2] / 1e3
+
+    if rank != 0:
+        return
+    hbm, bf16, src = peaks()
+    steps = args.steps
+    qps = ws * N_QUERIES * steps / ours["t_query"]
+    tps = ws * N_TRAIN * steps / ours["t_train"]
+    p_steps = max(1, min(args.steps, 3)) if path != nmg.PATH_FP32 else steps
+    plain_qps = N_QUERIES * p_steps / plain["t_query"]
+    plain_tps = N_TRAIN * p_steps / plain["t_train"]
+    tflops = FLOP_PER_QUERY * N_QUERIES / t_kernel / 1e12
+    gbs = BYTES_PER_QUERY * N_QUERIES / t_kernel / 1e9
+    cpu = cpu_baseline(q, x, rec, seconds=args.cpu_seconds) if not args.no_cpu else None
+    line = {
+        "metric": "guided queries/s & train samples/s, BF16 fused vs FP32 plain, 1 GB300",
+        "value": qps,
+        "unit": "queries/s",
+        "n_gpus": ws,
+        "steps": steps,
+        "warmup": args.warmup,
+        "ms_per_step": (ours["t_query"] + ours["t_train"]) / steps * 1e3,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": {"bf16": "bf16", "fp16": "fp16", "fp32": "f32"}[args.path],
+        "data": "synthetic (seeded wavefront + ground-truth radiance field; no scene data)",
+        "config": {"workload": "full guiding step: 2,073,600-query wavefront (1920x1080) + 2^18-sample train step",
+                   "network": "hash grid 16x2 (2^19/level, base 16, x1.447) + SH4(wo) + SH4(n) + OneBlob4(r) "
+                              "-> 80-64-64-64-48 MLP, K=8 lobes + selection",
+                   "path": args.path, "l2": "flushed (256 MiB write) before each timed step",
+                   "parallelism": "replicas" if ws > 1 else "single GPU"},
+        "train_samples_per_s": tps,
+        "query_ms": ours["t_query"] / steps * 1e3,
+        "train_ms": ours["t_train"] / steps * 1e3,
+        "plain_fp32": {"queries_per_s": plain_qps, "train_samples_per_s": plain_tps,
+                       "query_ms": plain["t_query"] / p_steps * 1e3, "train_ms": plain["t_train"] / p_steps * 1e3},
+        "speedup_vs_plain_fp32": {"queries": qps / ws / plain_qps, "train": tps / ws / plain_tps},
+        "final_stats": {"mean_loss": ours["loss"][0], "grad_norm": ours["loss"][1]},
+        "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s (query + train step, host buffers)",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": None,
+        "roofline": {"kernel": "k_fused_query" if path != nmg.PATH_FP32 else "plain query kernels",
+                     "bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",
+                     "frac": tflops / bf16, "peak_source": src, "traffic": None,
+                     "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm,
+                     "per_unit": {"flop_per_query": FLOP_PER_QUERY, "hbm_bytes_per_query": BYTES_PER_QUERY},
+                     "kernel_ms": t_kernel * 1e3},
+        "cpu_baseline": cpu,
+        "clocks": ours["clocks"],
+    }
+    line["gpu_launches"] = launches_per_step(path) * steps
+    print(json.dumps(line), flush=True)
+
+
+def launches_per_step(path):
+    """Kernels of this library launched per timed step (query pass + train step)."""
+    if path == 0:
+        # query: featurize, encode, 4 linear, mixture; train: encode, 4 linear, loss, 4x(wgrad+dgrad),
+        # grid scatter, step counter, adam, stats
+        return 7 + (1 + 4 + 1 + 8 + 1 + 1 + 1 + 1)
+    return 1 + FUSED_TRAIN_LAUNCHES
+
+
+FUSED_TRAIN_LAUNCHES = 21
+
+
+def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
+    """The guiding step restated on the host (oracle/, OpenMP), on a bounded sample."""
+    import numpy as np
+
+    import oracle as O
+    nmg = importlib.import_module(PKG)
+    cfg = nmg.config(nmg.PRESET_HASHGRID)
+    net = O.make_net(**nmg.oracle_net_spec(cfg))
+    rng = np.random.default_rng(0)
+    params = np.zeros(net.n_params, np.float32)
+    params[:net.n_mlp_params] = rng.uniform(-0.15, 0.15, net.n_mlp_params)
+    params[net.n_mlp_params:] = rng.uniform(-1e-4, 1e-4, net.n_params - net.n_mlp_params)
+    # query sample
+    n = 4096
+    t0 = time.perf_counter()
+    done = 0
+    while time.perf_counter() - t0 < seconds / 2 or done == 0:
+        sl = slice(done % (N_QUERIES - n), done % (N_QUERIES - n) + n)
+        xi = O.featurize(net, q["pos"][sl], q["wo"][sl], q["normal"][sl], q["rough"][sl], q["aabb"])
+        raw = O.network_forward(net, params, xi).astype(np.float32)
+        s = np.where((q["normal"][sl] * q["wo"][sl]).sum(1, keepdims=True) > 0, 1.0, -1.0).astype(np.float32)
+        O.mixture_sample(raw, 8, q["u4"][sl], q["normal"][sl] * s, fp64=False)
+        done += n
+    tq = time.perf_counter() - t0
+    # train sample
+    m = 2048
+    t1 = time.perf_counter()
+    tdone = 0
+    while time.perf_counter() - t1 < seconds / 2 or tdone == 0:
+        sl = slice(tdone % (N_TRAIN - m), tdone % (N_TRAIN - m) + m)
+        raw = O.network_forward(net, params, x[sl]).astype(np.float32)
+        g, _, _ = O.mixture_loss_grad(raw, 8, rec[sl], 128.0, selection=True, fp64=False)
+        O.network_backward(net, params, x[sl], g)
+        tdone += m
+    tt = time.perf_counter() - t1
+    # Adam over all parameters once per step, timed separately and amortised per sample of a 2^18 batch
+    w = params.copy()
+    mm, vv = np.zeros_like(w), np.zeros_like(w)
+    ps, ema = np.zeros(w.size, np.uint32), w.copy()
+    gr = np.zeros_like(w)
+    ta = time.perf_counter()
+    O.adam_ema(gr, 128.0, 1e-2, 0.9, 0.99, 1e-15, 1e-6, 0.95, 1, w, mm, vv, ps, ema, net.n_mlp_params)
+    ta = time.perf_counter() - ta
+    per_sample = tt / tdone + ta / N_TRAIN
+    return {"value": done / tq, "unit": "queries/s", "train_samples_per_s": 1.0 / per_sample,
+            "cores": O.num_threads(), "kind": kind,
+            "sample": "%d queries and %d training samples of the same workload (FP32 reference-order mixture, "
+                      "FP64 restated encoding+MLP, OpenMP)" % (done, tdone)}
+
+
+def run_reference(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import numpy as np
+    synth = importlib.import_module(PKG + ".synth")
+    q = synth.wavefront(N_QUERIES, seed=7272)
+    field = synth.TrainField(seed=7272)
+    x, rec = synth.train_batch(field, N_TRAIN, seed=7273, input_mode=1, selection=True)
+    per = max(2.0, 60.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        cpu_baseline(q, x, rec, seconds=1.0)
+    t0 = time.perf_counter()
+    vals, tvals, last = [], [], None
+    for _ in range(args.steps):
+        last = cpu_baseline(q, x, rec, seconds=per)
+        vals.append(last["value"])
+        tvals.append(last["train_samples_per_s"])
+    wall = time.perf_counter() - t0
+    v = float(np.mean(vals))
+    line = {
+        "impl": "reference",
+        "metric": "guided queries/s & train samples/s, BF16 fused vs FP32 plain, 1 GB300",
+        "value": v, "unit": "queries/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall / max(1, args.steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded wavefront + ground-truth radiance field)",
+        "config": {"workload": "full guiding step: 2,073,600-query wavefront (1920x1080) + 2^18-sample train step",
+                   "sample": "bounded per step; throughput scaled to the unit"},
+        "train_samples_per_s": float(np.mean(tvals)),
+        "cpu_baseline": {"value": v, "unit": "queries/s", "cores": last["cores"], "kind": "port",
+                         "sample": last["sample"]},
+        "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="bf16", choices=["bf16", "fp16", "fp32"])
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

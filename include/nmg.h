@@ -279,6 +279,11 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
 nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int n, float* raw, float* dparams,
                            nmg_stream stream);
 
+/* Synchronises the device and reports an error recorded by a kernel of this
+ * context since the last check (NMG_ERR_TIMEOUT when a bounded device wait
+ * gave up). */
+nmg_status nmg_check_errors(nmg_ctx* ctx);
+
 /* Host-file checkpoint of {master params, inference params, Adam moments,
  * step counters, step}. */
 nmg_status nmg_save(const nmg_ctx* ctx, const char* path);

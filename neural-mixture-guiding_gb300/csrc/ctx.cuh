@@ -33,8 +33,9 @@ struct Workspace {
   float* dh[2] = {};       // [cap_b][max(64, n_enc_pad)] ping-pong deltas
   double* partials = nullptr;  // block partial sums (loss, grad norm)
   int n_partials = 0;
-  // fused path
+  // fused path: host-side state object and its device allocation
   void* fused = nullptr;
+  void* fused_dev = nullptr;
   size_t fused_bytes = 0;
 };
 
@@ -87,6 +88,9 @@ nmg_status fused_query(nmg_ctx* c, const nmg_shading* in, const float* u4, const
                        const nmg_query_out* out, cudaStream_t st);
 nmg_status fused_infer_raw(nmg_ctx* c, const float* x, const int* d_count, int n_max, int which, float* raw,
                            cudaStream_t st);
+nmg_status pack_images(nmg_ctx* c, cudaStream_t st);
+void fused_release(nmg_ctx* c);
+nmg_status fused_check_errors(nmg_ctx* c);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st);
 

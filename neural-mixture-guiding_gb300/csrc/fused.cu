@@ -1,15 +1,532 @@
-// fused.cu -- placeholder until the tcgen05 kernels land.
+// fused.cu -- the fused reduced-precision guiding step on the sm_103a tensor
+// cores: one persistent kernel per wavefront does
+//   featurise -> encode (grid gathers + SH + one-blob, BF16/FP16 into a
+//   shared-memory operand tile) -> MLP on tcgen05 (FP32 accumulators in TMEM,
+//   ReLU epilogues back to shared memory) -> mixture activation, cosine lobe,
+//   lobe selection, vMF sample and pdf (FP32, registers).
+//
+// CTA organisation (one CTA per SM, 512 threads): four independent
+// warpgroups, each owning a 128-query tile at a time, its operand tiles in
+// shared memory, a TMEM accumulator slice and an mbarrier. Thread t of a
+// warpgroup owns row t of the tile: it encodes the row, reads the row back
+// from TMEM lanes (warp w of the group reads lanes 32w..32w+31) and runs the
+// mixture for that query. The weights of all layers (32 KB for the hash-grid
+// network) are copied once per CTA into shared memory by a bulk copy
+// (cp.async.bulk) from a pre-packed image in core-matrix order and stay
+// resident. One elected thread per warpgroup issues that group's MMAs and
+// commits them to the group's mbarrier.
+//
+// Matches the reference semantics of the plain path (encoding grid.h,
+// spherical_harmonics.h, oneblob.h; MLP fully_fused_mlp.cu; mixture
+// distribution.h / vmf.h) up to the BF16/FP16 rounding of features,
+// weights and activations, and fast-math transcendental functions.
+#include <stdio.h>
+#include <string.h>
+
 #include "api_common.cuh"
 #include "ctx.cuh"
+#include "tcgen05.cuh"
+
 namespace nmg {
-nmg_status fused_reserve(nmg_ctx*) { return NMG_OK; }
-nmg_status fused_query(nmg_ctx*, const nmg_shading*, const float*, const int*, int, const nmg_query_out*, cudaStream_t) {
-  return set_error(NMG_ERR_UNSUPPORTED, "fused path not built");
+
+constexpr int kWG = 4;          // warpgroups per CTA
+constexpr int kRows = 128;      // rows per tile (MMA M)
+
+struct FusedArgs {
+  EncodingParams enc;
+  MixOpts mix;
+  const uint8_t* wimg;               // packed weight image
+  uint32_t w_bytes;                  // image bytes (multiple of 16)
+  uint32_t layer_off[kMaxLayers];    // byte offset of each layer in the image
+  int n_layers;
+  int fp16;                          // operands FP16 instead of BF16
+  const uint16_t* table;             // 16-bit grid table [entries][F]
+  uint32_t lvl_T[kMaxLevels];        // entries per level
+  uint32_t lvl_hash;                 // bit l: level l is hashed (res^3 > T, T a power of two)
+  int raw_mode;                      // 1: inputs are network input rows x, output raw only
+  int n_out;                         // used outputs (4K [+1])
+  int n_out_pad;
+  int selection;
+  const float* pos;
+  const float* wo;
+  const float* nrm;
+  const float* rough;
+  const float* u4;
+  const float* x;
+  const int* d_count;
+  int n_max;
+  float* dir;
+  float* pdf;
+  int* lobe;
+  float* raw;
+  float* sel;
+  int* err;
+};
+
+NMG_D int fused_count(const int* d_count, int n_max) {
+  if (!d_count) return n_max;
+  int n = *d_count;
+  return n < 0 ? 0 : (n > n_max ? n_max : n);
 }
-nmg_status fused_infer_raw(nmg_ctx*, const float*, const int*, int, int, float*, cudaStream_t) {
-  return set_error(NMG_ERR_UNSUPPORTED, "fused path not built");
+
+NMG_D bool bar_red_and(int id, int count, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred pin, pout;\n\t"
+      "setp.ne.u32 pin, %1, 0;\n\t"
+      "bar.red.and.pred pout, %2, %3, pin;\n\t"
+      "selp.u32 %0, 1, 0, pout;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(v)), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
 }
+
+NMG_D uint32_t level_index(const FusedArgs& a, int l, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t T = a.lvl_T[l];
+  if ((a.lvl_hash >> l) & 1u) return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (T - 1u);
+  const uint32_t res = a.enc.res[l];
+  uint32_t idx = x + y * res + z * (res * res);
+  return idx < T ? idx : (idx < 2u * T ? idx - T : idx % T);
+}
+
+template <int BINS>
+NMG_D void oneblob_fixed(float x, float* o) {
+  const float nb = float(BINS);
+  float left = quartic_cdf(-x, nb) + quartic_cdf(-x - 1.f, nb) + quartic_cdf(-x + 1.f, nb);
+#pragma unroll
+  for (int k = 0; k < BINS; ++k) {
+    const float rb = float(k + 1) / nb;
+    float right = quartic_cdf(rb - x, nb) + quartic_cdf(rb - x - 1.f, nb) + quartic_cdf(rb - x + 1.f, nb);
+    o[k] = right - left;
+    left = right;
+  }
+}
+
+NMG_D void store_chunk(uint8_t* tile, int row, int chunk, int chunks, const float* f, bool fp16) {
+  uint4 v;
+  v.x = tc::pack2(f[0], f[1], fp16);
+  v.y = tc::pack2(f[2], f[3], fp16);
+  v.z = tc::pack2(f[4], f[5], fp16);
+  v.w = tc::pack2(f[6], f[7], fp16);
+  *reinterpret_cast<uint4*>(tile + tc::cm_offset(row, chunk, chunks)) = v;
+}
+
+template <int F>
+NMG_D void load_feats(const uint16_t* table, uint32_t entry, float* v, bool fp16) {
+  if (F == 2) {
+    uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(table) + entry);
+    float2 p = tc::unpack2(w, fp16);
+    v[0] = p.x;
+    v[1] = p.y;
+  } else {
+    uint2 w = __ldg(reinterpret_cast<const uint2*>(table) + entry);
+    float2 p = tc::unpack2(w.x, fp16), q = tc::unpack2(w.y, fp16);
+    v[0] = p.x;
+    v[1] = p.y;
+    v[2] = q.x;
+    v[3] = q.y;
+  }
+}
+
+// Encodes one input row x into `tile` row `row` (KC 16-byte chunks).
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS>
+NMG_D void encode_row(const FusedArgs& a, const float* x, uint8_t* tile, int row) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NGRID = LEVELS * F;
+  constexpr int NPAD = (NGRID + NDIR + 15) / 16 * 16;
+  constexpr int KC = NPAD / 8;
+  constexpr int LPC = 8 / F;
+  static_assert(NGRID % 8 == 0, "grid features must fill whole chunks");
+  const bool fp16 = a.fp16 != 0;
+  const float p3[3] = {x[0], x[1], x[2]};
+#pragma unroll
+  for (int ch = 0; ch < NGRID / 8; ++ch) {
+    float f[8];
+#pragma unroll
+    for (int j = 0; j < LPC; ++j) {
+      const int l = ch * LPC + j;
+      float w[3];
+      uint32_t g[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[l], a.enc.smoothstep, &w[d], &g[d]);
+      float acc[F];
+#pragma unroll
+      for (int k = 0; k < F; ++k) acc[k] = 0.f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const float wt = ((c & 1) ? w[0] : 1.f - w[0]) * ((c & 2) ? w[1] : 1.f - w[1]) * ((c & 4) ? w[2] : 1.f - w[2]);
+        const uint32_t e = a.enc.offset[l] +
+                           level_index(a, l, g[0] + (c & 1), g[1] + ((c >> 1) & 1), g[2] + ((c >> 2) & 1));
+        float v[F];
+        load_feats<F>(a.table, e, v, fp16);
+#pragma unroll
+        for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < F; ++k) f[j * F + k] = acc[k];
+    }
+    store_chunk(tile, row, ch, KC, f, fp16);
+  }
+  float d[NPAD - NGRID];
+  sh_basis(SHDEG, x[3] * 2.f - 1.f, x[4] * 2.f - 1.f, x[5] * 2.f - 1.f, d);
+  if (MODE == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) oneblob_fixed<BINS>(x[6 + k], d + SHDEG * SHDEG + k * BINS);
+  } else {
+    sh_basis(SHDEG, x[6] * 2.f - 1.f, x[7] * 2.f - 1.f, x[8] * 2.f - 1.f, d + SHDEG * SHDEG);
+    oneblob_fixed<BINS>(x[9], d + 2 * SHDEG * SHDEG);
+  }
+#pragma unroll
+  for (int k = NDIR; k < NPAD - NGRID; ++k) d[k] = 1.f;
+#pragma unroll
+  for (int ch = 0; ch < (NPAD - NGRID) / 8; ++ch) store_chunk(tile, row, NGRID / 8 + ch, KC, d + 8 * ch, fp16);
+}
+
+NMG_D f3 face_fwd(f3 n, f3 v) { return dot3(n, v) > 0.f ? n : f3{-n.x, -n.y, -n.z}; }
+
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+__global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_constant__ FusedArgs a) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
+  constexpr uint32_t A_BYTES = kRows * NENC * 2;
+  constexpr uint32_t H_BYTES = kRows * kWidth * 2;
+  constexpr uint32_t COLS = NOUTMAX <= 64 ? 64 : 128;  // TMEM columns per warpgroup
+  extern __shared__ __align__(1024) uint8_t smem[];
+
+  const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
+  const int wg = threadIdx.x / kRows, t = threadIdx.x % kRows, warp_in_wg = t / 32;
+  uint8_t* wsm = smem;
+  uint8_t* A = smem + w_region + wg * (A_BYTES + H_BYTES);
+  uint8_t* H = A + A_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + kWG * (A_BYTES + H_BYTES));
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
+
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bars[0], 1);
+    for (int g = 0; g < kWG; ++g) tc::mbar_init(&bars[1 + g], 1);
+    tc::fence_mbar_init();
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(tslot, COLS * kWG);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&bars[0], a.w_bytes);
+    for (uint32_t off = 0; off < a.w_bytes; off += 16384u) {
+      const uint32_t nb = a.w_bytes - off < 16384u ? a.w_bytes - off : 16384u;
+      tc::bulk_g2s(wsm + off, a.wimg + off, nb, &bars[0]);
+    }
+  }
+  bool ok = tc::mbar_wait(&bars[0], 0);
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(a.err, 1);
+
+  const uint32_t tmem = *tslot + uint32_t(wg) * COLS;
+  const uint32_t lane_addr = tmem + (uint32_t(warp_in_wg * 32) << 16);
+  uint64_t* bar = &bars[1 + wg];
+  uint32_t phase = 0;
+  const bool fp16 = a.fp16 != 0;
+  const int n = fused_count(a.d_count, a.n_max);
+  const int ntiles = (n + kRows - 1) / kRows;
+  const int nl = a.n_layers;
+
+  // Every early exit below follows a warpgroup-wide bar.red.and, so the 128
+  // threads of a group always leave the loop together (no thread can be
+  // left waiting at a named barrier).
+  for (int tile = blockIdx.x * kWG + wg; tile < ntiles; tile += gridDim.x * kWG) {
+    const long q = long(tile) * kRows + t;
+    const bool valid = q < n;
+    // ---- encode this thread's row into A
+    float x[10];
+#pragma unroll
+    for (int d = 0; d < 10; ++d) x[d] = 0.f;
+    if (valid) {
+      if (a.raw_mode) {
+        for (int d = 0; d < a.enc.n_input; ++d) x[d] = a.x[q * a.enc.n_input + d];
+      } else {
+        featurize(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
+      }
+    }
+    encode_row<F, LEVELS, MODE, SHDEG, BINS>(a, x, A, t);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    ok = bar_red_and(1 + wg, kRows, ok);
+    if (!ok) break;
+    // ---- MLP: layer l reads A (l == 0) or H, writes TMEM; hidden layers go back to H
+    float r[NOUTMAX];
+    bool last_ok = true;
+    for (int l = 0; l < nl; ++l) {
+      const bool last = l == nl - 1;
+      const int kin = l == 0 ? NENC : kWidth;
+      const int nout = last ? a.n_out_pad : kWidth;
+      if (t == 0) {
+        tc::fence_after_sync();
+        const uint32_t a_addr = tc::smem_u32(l == 0 ? A : H);
+        const uint32_t b_addr = tc::smem_u32(wsm) + a.layer_off[l];
+        const uint32_t sbo = uint32_t(kin / 8) * 128u;
+        const uint32_t idesc = tc::idesc_f16(kRows, nout, fp16);
+        for (int kk = 0; kk < kin / 16; ++kk)
+          tc::mma_f16(tmem, tc::smem_desc(a_addr + kk * 256u, 128u, sbo), tc::smem_desc(b_addr + kk * 256u, 128u, sbo),
+                      idesc, kk > 0 ? 1u : 0u);
+        tc::mma_commit(bar);
+      }
+      const bool done = tc::mbar_wait(bar, phase);
+      phase ^= 1u;
+      tc::fence_after_sync();
+      if (!last) {
+        float v[kWidth];
+#pragma unroll
+        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(lane_addr + c * 16, v + 16 * c);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int c = 0; c < kWidth / 8; ++c) {
+          float f[8];
+#pragma unroll
+          for (int i = 0; i < 8; ++i) f[i] = fmaxf(v[8 * c + i], 0.f);
+          store_chunk(H, t, c, kWidth / 8, f, fp16);
+        }
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        ok = bar_red_and(1 + wg, kRows, done);
+        if (!ok) break;
+      } else {
+#pragma unroll
+        for (int c = 0; c < NOUTMAX / 16; ++c)
+          if (c * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + c * 16, r + 16 * c);
+        tc::tmem_wait_ld();
+        last_ok = done;
+      }
+    }
+    if (!ok) break;
+    ok = last_ok;  // reconciled across the group at the next tile's barrier
+    // ---- epilogue: raw outputs and/or mixture
+    if (valid && ok) {
+      if (a.raw) {
+        float4* dst = reinterpret_cast<float4*>(a.raw + q * a.n_out_pad);
+#pragma unroll
+        for (int c = 0; c < NOUTMAX / 4; ++c)
+          if (c * 4 < a.n_out_pad) dst[c] = make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+      }
+      if (!a.raw_mode) {
+        Mix<K> m;
+        mix_activate_regs<K, true>(m, r, a.mix.kappa_softplus);
+        if (a.mix.cosine) mix_apply_cosine<K, true>(m, face_fwd(load3(a.nrm, q), load3(a.wo, q)));
+        const float4 u = reinterpret_cast<const float4*>(a.u4)[q];
+        const int s = mix_select<K>(m, u.y);
+        const f3 dv = mix_sample_lobe<K, true>(m, s, u.z, u.w);
+        store3(a.dir, q, dv);
+        a.pdf[q] = mix_pdf<K, true>(m, dv);
+        if (a.lobe) a.lobe[q] = s;
+        if (a.sel && a.selection) a.sel[q] = logistic<true>(r[4 * K < NOUTMAX ? 4 * K : 0]);
+      }
+    }
+  }
+  if (!ok && t == 0) atomicExch(a.err, 2);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(*tslot, COLS * kWG);
+  }
+}
+
+// ------------------------------------------------------------ weight image
+// Element (n, k) of layer l goes to byte layer_off[l] + cm_offset(n, k/8,
+// in_l/8) + 2 (k % 8): each layer becomes a K-major operand of N = out_l rows.
+struct PackArgs {
+  long off[kMaxLayers + 1];
+  int in[kMaxLayers];
+  uint32_t layer_off[kMaxLayers];
+  int n_layers;
+};
+
+__global__ void k_pack_weights(PackArgs p, const uint16_t* __restrict__ w16, uint16_t* __restrict__ img) {
+  const long total = p.off[p.n_layers];
+  for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += long(gridDim.x) * blockDim.x) {
+    int l = 0;
+    while (l + 1 < p.n_layers && i >= p.off[l + 1]) ++l;
+    const long j = i - p.off[l];
+    const int in = p.in[l];
+    const int nrow = int(j / in), k = int(j % in);
+    const uint32_t b = p.layer_off[l] + tc::cm_offset(nrow, k >> 3, in >> 3) + uint32_t(k & 7) * 2u;
+    img[b >> 1] = w16[i];
+  }
+}
+
+// ------------------------------------------------------------------- host
+struct FusedState {
+  uint8_t* img_train;
+  uint8_t* img_infer;
+  int* err;
+  uint32_t w_bytes;
+  PackArgs pack;
+  int preset;  // 0 none, 1 hash-grid K8, 2 hash-grid K16, 3 reference K8
+};
+
+static FusedState* fstate(nmg_ctx* c) { return reinterpret_cast<FusedState*>(c->ws.fused); }
+
+static int preset_of(const nmg_ctx* c) {
+  const nmg_config& g = c->cfg;
+  const bool hash = g.input_mode == 1 && g.grid_features == 2 && g.grid_levels == 16 && g.sh_degree == 4 &&
+                    g.oneblob_bins == 4;
+  const bool ref = g.input_mode == 0 && g.grid_features == 4 && g.grid_levels == 8 && g.sh_degree == 2 &&
+                   g.oneblob_bins == 4;
+  if (hash && g.n_lobes == 8) return 1;
+  if (hash && g.n_lobes == 16) return 2;
+  if (ref && g.n_lobes == 8 && !g.selection) return 3;
+  return 0;
+}
+
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+static size_t smem_bytes_for(uint32_t w_bytes) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
+  return size_t((w_bytes + 1023u) & ~1023u) + kWG * (size_t(kRows) * NENC * 2 + size_t(kRows) * kWidth * 2) + 128;
+}
+
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+static nmg_status launch_query(const FusedArgs& a, cudaStream_t st) {
+  auto kern = k_fused_query<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX>;
+  const size_t smem = smem_bytes_for<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX>(a.w_bytes);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "fused query smem %zu: %s", smem, cudaGetErrorString(e));
+  int sms = 152;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const int tiles = (a.n_max + kRows - 1) / kRows;
+  int grid = (tiles + kWG - 1) / kWG;
+  if (grid > sms) grid = sms;
+  if (grid < 1) grid = 1;
+  kern<<<grid, kWG * kRows, smem, st>>>(a);
+  return check_launch("k_fused_query");
+}
+
+static nmg_status dispatch_query(nmg_ctx* c, const FusedArgs& a, cudaStream_t st) {
+  switch (fstate(c)->preset) {
+    case 1: return launch_query<2, 16, 1, 4, 4, 8, 48>(a, st);
+    case 2: return launch_query<2, 16, 1, 4, 4, 16, 80>(a, st);
+    case 3: return launch_query<4, 8, 0, 2, 4, 8, 48>(a, st);
+  }
+  return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
+}
+
+nmg_status pack_images(nmg_ctx* c, cudaStream_t st) {
+  FusedState* s = fstate(c);
+  if (!s) return NMG_OK;
+  k_pack_weights<<<64, 256, 0, st>>>(s->pack, c->w16, reinterpret_cast<uint16_t*>(s->img_train));
+  k_pack_weights<<<64, 256, 0, st>>>(s->pack, c->w16_inf, reinterpret_cast<uint16_t*>(s->img_infer));
+  return check_launch("k_pack_weights");
+}
+
+nmg_status fused_reserve(nmg_ctx* c) {
+  const int preset = preset_of(c);
+  if (!preset) return NMG_OK;  // fused calls will report UNSUPPORTED
+  const Layout& L = c->lay;
+  FusedState s{};
+  s.preset = preset;
+  uint32_t off = 0;
+  s.pack.n_layers = L.n_layers;
+  for (int l = 0; l < L.n_layers; ++l) {
+    s.pack.off[l] = L.off[l];
+    s.pack.in[l] = L.in[l];
+    s.pack.layer_off[l] = off;
+    off += uint32_t(L.in[l]) * uint32_t(L.out[l]) * 2u;
+  }
+  s.pack.off[L.n_layers] = L.off[L.n_layers];
+  s.w_bytes = (off + 15u) & ~15u;
+  const size_t head = 256;
+  const size_t bytes = head + 2 * size_t(s.w_bytes);
+  void* mem = nullptr;
+  cudaError_t e = cudaMalloc(&mem, bytes);
+  if (e != cudaSuccess) return set_error(NMG_ERR_OOM, "fused workspace: %s", cudaGetErrorString(e));
+  cudaMemset(mem, 0, bytes);
+  // the state struct lives on the host; its device buffers follow a 256-byte header
+  FusedState* hs = new FusedState(s);
+  hs->err = reinterpret_cast<int*>(mem);
+  hs->img_train = reinterpret_cast<uint8_t*>(mem) + head;
+  hs->img_infer = hs->img_train + s.w_bytes;
+  c->ws.fused_dev = mem;
+  c->ws.fused = hs;
+  c->ws.fused_bytes = bytes;
+  return pack_images(c, 0);
+}
+
+void fused_release(nmg_ctx* c) {
+  delete fstate(c);
+  c->ws.fused = nullptr;
+}
+
+static FusedArgs make_args(nmg_ctx* c, bool infer_weights) {
+  FusedState* s = fstate(c);
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.enc = c->enc;
+  a.mix = c->mix;
+  a.wimg = infer_weights ? s->img_infer : s->img_train;
+  a.w_bytes = s->w_bytes;
+  for (int l = 0; l < c->lay.n_layers; ++l) a.layer_off[l] = s->pack.layer_off[l];
+  a.n_layers = c->lay.n_layers;
+  a.fp16 = c->cfg.path == NMG_PATH_FP16;
+  a.table = (infer_weights ? c->w16_inf : c->w16) + c->lay.n_mlp;
+  a.lvl_hash = 0;
+  for (int l = 0; l < c->enc.levels; ++l) {
+    const uint32_t T = c->enc.offset[l + 1] - c->enc.offset[l];
+    a.lvl_T[l] = T;
+    const unsigned long long r = c->enc.res[l];
+    if (c->enc.grid_hash && r * r * r > T) a.lvl_hash |= 1u << l;
+  }
+  a.n_out = c->lay.n_out;
+  a.n_out_pad = c->lay.n_out_pad;
+  a.selection = c->cfg.selection;
+  a.err = s->err;
+  return a;
+}
+
+nmg_status fused_query(nmg_ctx* c, const nmg_shading* in, const float* u4, const int* d_count, int n_max,
+                       const nmg_query_out* out, cudaStream_t st) {
+  if (!fstate(c)) return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
+  FusedArgs a = make_args(c, true);
+  a.pos = in->pos;
+  a.wo = in->wo;
+  a.nrm = in->normal;
+  a.rough = in->roughness;
+  a.u4 = u4;
+  a.d_count = d_count;
+  a.n_max = n_max;
+  a.dir = out->dir;
+  a.pdf = out->pdf;
+  a.lobe = out->lobe;
+  a.raw = out->raw;
+  a.sel = out->selection;
+  return dispatch_query(c, a, st);
+}
+
+nmg_status fused_infer_raw(nmg_ctx* c, const float* x, const int* d_count, int n_max, int which, float* raw,
+                           cudaStream_t st) {
+  if (!fstate(c)) return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
+  FusedArgs a = make_args(c, which == 1);
+  a.raw_mode = 1;
+  a.x = x;
+  a.d_count = d_count;
+  a.n_max = n_max;
+  a.raw = raw;
+  return dispatch_query(c, a, st);
+}
+
+nmg_status fused_check_errors(nmg_ctx* c) {
+  FusedState* s = fstate(c);
+  if (!s) return NMG_OK;
+  int e = 0;
+  NMG_CUDA_TRY(cudaMemcpy(&e, s->err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    cudaMemset(s->err, 0, sizeof(int));
+    return set_error(NMG_ERR_TIMEOUT, "a fused kernel gave up waiting (code %d)", e);
+  }
+  return NMG_OK;
+}
+
 nmg_status fused_train_step(nmg_ctx*, const float*, const float*, const int*, int, double*, cudaStream_t) {
-  return set_error(NMG_ERR_UNSUPPORTED, "fused path not built");
+  return set_error(NMG_ERR_UNSUPPORTED, "fused training step not built yet");
 }
+
 }  // namespace nmg

@@ -28,7 +28,11 @@ template <bool FAST> NMG_D float xdiv(float a, float b) { return FAST ? __fdivid
 // train.h:391-415 activations.
 NMG_D float act_exp_clamp(float x) { return fminf(fmaxf(x, -10.f), 15.f); }
 template <bool FAST> NMG_D float logistic(float x) { return xdiv<FAST>(1.f, 1.f + xexp<FAST>(-x)); }
-template <bool FAST> NMG_D float softplus(float x) { return FAST ? __logf(1.f + __expf(x)) : logf(1.f + expf(x)); }
+// Softplus in the stable form max(x,0) + log1p(e^-|x|) (train.h:398 writes
+// log(1+e^x), which loses all digits for x < -16).
+template <bool FAST> NMG_D float softplus(float x) {
+  return fmaxf(x, 0.f) + log1pf(xexp<FAST>(-fabsf(x)));
+}
 
 struct MixOpts {
   int kappa_softplus;  // 0: kappa = exp(clamp(x)) (train.h:244); 1: log(1+e^x)
@@ -46,8 +50,11 @@ template <int K> struct Mix {
 
 // vMF normaliser k / (2 pi (1 - e^{-2k})) (vmf.h:25-26); below M_EPSILON the
 // lobe is uniform (1/4pi).
+// The denominator uses -expm1(-2k) below k = 0.5, where 1 - e^{-2k} cancels.
 template <bool FAST> NMG_D float vmf_norm(float k) {
-  return k < NMG_EPS ? NMG_INV_4PI : xdiv<FAST>(k, NMG_TWO_PI * (1.f - xexp<FAST>(-2.f * k)));
+  if (k < NMG_EPS) return NMG_INV_4PI;
+  const float den = k < 0.5f ? -expm1f(-2.f * k) : 1.f - xexp<FAST>(-2.f * k);
+  return xdiv<FAST>(k, NMG_TWO_PI * den);
 }
 
 // distribution.h:85-98: activation of one query's raw outputs. `raw` points
@@ -72,6 +79,28 @@ NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
   for (int i = 0; i < K; ++i) m.w[i] = m.lam[i] / m.total;
 }
 
+// Same activation from raw outputs held in registers (compile-time indices).
+template <int K, bool FAST, int N>
+NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplus) {
+  static_assert(N >= 4 * K, "raw row too short");
+  m.total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    m.lam[i] = xexp<FAST>(act_exp_clamp(raw[4 * i]));
+    m.kap[i] = kappa_softplus ? softplus<FAST>(raw[4 * i + 1]) : xexp<FAST>(act_exp_clamp(raw[4 * i + 1]));
+    float th = NMG_PI * logistic<FAST>(raw[4 * i + 2]);
+    float ph = NMG_TWO_PI * logistic<FAST>(raw[4 * i + 3]);
+    float st, ct, sp, cp;
+    xsincos<FAST>(th, &st, &ct);
+    xsincos<FAST>(ph, &sp, &cp);
+    m.mu[i] = f3{st * cp, st * sp, ct};
+    m.total += m.lam[i];
+  }
+  const float inv = 1.f / m.total;
+#pragma unroll
+  for (int i = 0; i < K; ++i) m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / m.total;
+}
+
 // distribution.h:39-64 + 184-195: product of every lobe with the cosine lobe
 // (kappa 2.18853) around `n` (already face-forwarded, any length), then
 // renormalisation with total clamped below at M_EPSILON.
@@ -80,7 +109,7 @@ NMG_D void mix_apply_cosine(Mix<K>& m, f3 n) {
   const float kb = 2.18853f;
   f3 mb = normalize3(n);
   auto pnorm = [](float k) {
-    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, 1.f - xexp<FAST>(-2.f * k));
+    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, -expm1f(-2.f * k));
   };
   const float nb = pnorm(kb);
   m.total = 0.f;
@@ -145,8 +174,22 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
     xsincos<FAST>(ph, &sp, &cp);
     return f3{r * cp, r * sp, z};
   }
-  float ct = 1.f + log1pf(-u0 + xexp<FAST>(-2.f * k) * u0) / k;
-  float st = sqrtf(fmaxf(0.f, 1.f - ct * ct));
+  // cos(theta) = 1 + log1p(-u0 + e^{-2k} u0) / k (vmf.h:51), evaluated as
+  // 1 - cos = -log1p(u0 expm1(-2k)) / k and, on the far hemisphere,
+  // 1 + cos = log1p((1 - u0) expm1(2k)) / k, so that sin^2 = (1-cos)(1+cos)
+  // keeps its digits near both poles of the lobe (k < 8.3 there, so
+  // expm1(2k) stays finite).
+  const float omc = -log1pf(u0 * expm1f(-2.f * k)) / k;
+  float ct, s2;
+  if (omc <= 1.f) {
+    ct = 1.f - omc;
+    s2 = omc * (2.f - omc);
+  } else {
+    const float opc = log1pf((1.f - u0) * expm1f(2.f * k)) / k;
+    ct = opc - 1.f;
+    s2 = opc * (2.f - opc);
+  }
+  float st = sqrtf(fmaxf(0.f, s2));
   xsincos<FAST>(ph, &sp, &cp);
   loc = f3{cp * st, sp * st, ct};
   // Frame(mu): T = normalize(mu x e), e the branchless axis pick; B = normalize(mu x T)
@@ -190,9 +233,8 @@ NMG_D float mix_kl_loss_grad(const float* raw, const float* rec, float scale, co
     float4 r = reinterpret_cast<const float4*>(raw)[i];
     lam[i] = xexp<FAST>(act_exp_clamp(r.x));
     if (o.kappa_softplus) {
-      float e = xexp<FAST>(r.y);
-      kap[i] = FAST ? __logf(1.f + e) : logf(1.f + e);
-      dkap[i] = xdiv<FAST>(e, e + 1.f);
+      kap[i] = softplus<FAST>(r.y);
+      dkap[i] = logistic<FAST>(r.y);
     } else {
       kap[i] = xexp<FAST>(act_exp_clamp(r.y));
       dkap[i] = kap[i];  // train.h:410: derivative ignores the clamp
@@ -269,9 +311,8 @@ NMG_D float mix_kl_loss_grad_selection(const float* raw, const float* rec, float
     float4 r = reinterpret_cast<const float4*>(raw)[i];
     lam[i] = xexp<FAST>(act_exp_clamp(r.x));
     if (o.kappa_softplus) {
-      float e = xexp<FAST>(r.y);
-      kap[i] = FAST ? __logf(1.f + e) : logf(1.f + e);
-      dkap[i] = xdiv<FAST>(e, e + 1.f);
+      kap[i] = softplus<FAST>(r.y);
+      dkap[i] = logistic<FAST>(r.y);
     } else {
       kap[i] = xexp<FAST>(act_exp_clamp(r.y));
       dkap[i] = kap[i];

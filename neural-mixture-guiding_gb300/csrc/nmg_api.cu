@@ -124,7 +124,10 @@ static nmg_status dalloc(T** p, size_t count) {
   return NMG_OK;
 }
 
-static void free_workspace(Workspace& w) {
+static void free_workspace(nmg_ctx* c) {
+  Workspace& w = c->ws;
+  fused_release(c);
+  cudaFree(w.fused_dev);
   cudaFree(w.x);
   cudaFree(w.enc);
   for (auto& h : w.h) cudaFree(h);
@@ -133,7 +136,6 @@ static void free_workspace(Workspace& w) {
   cudaFree(w.dh[0]);
   cudaFree(w.dh[1]);
   cudaFree(w.partials);
-  cudaFree(w.fused);
   w = Workspace();
 }
 
@@ -143,7 +145,7 @@ static nmg_status reserve(nmg_ctx* c, int max_q, int max_b) {
   max_q = max_q > w.cap_q ? max_q : w.cap_q;
   max_b = max_b > w.cap_b ? max_b : w.cap_b;
   cudaDeviceSynchronize();
-  free_workspace(w);
+  free_workspace(c);
   const int cap = max_q > max_b ? max_q : max_b;
   const Layout& L = c->lay;
   const size_t capz = size_t(cap > 1 ? cap : 1);
@@ -307,7 +309,7 @@ nmg_status nmg_create(const nmg_config* cfg, nmg_ctx** out) {
 void nmg_destroy(nmg_ctx* c) {
   if (!c) return;
   cudaDeviceSynchronize();
-  free_workspace(c->ws);
+  free_workspace(c);
   if (c->w_inf != c->w) cudaFree(c->w_inf);
   cudaFree(c->w);
   cudaFree(c->grad);
@@ -432,6 +434,12 @@ nmg_status nmg_network_vjp(nmg_ctx* c, const float* x, const float* draw, int n,
   nmg_status s = need(c, n, true);
   if (s != NMG_OK || n == 0) return s;
   return plain_vjp(c, x, draw, n, raw, dparams, (cudaStream_t)stream);
+}
+
+nmg_status nmg_check_errors(nmg_ctx* c) {
+  NMG_REQUIRE(c != nullptr, "ctx is NULL");
+  NMG_CUDA_TRY(cudaDeviceSynchronize());
+  return fused_check_errors(c);
 }
 
 static const uint32_t kMagic = 0x31474d4e;  // "NMG1"

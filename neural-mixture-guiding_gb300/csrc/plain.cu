@@ -581,7 +581,8 @@ nmg_status sync_copies(nmg_ctx* c, cudaStream_t st) {
   if (!c->w16) return NMG_OK;
   k_sync_copies<<<152 * 8, 256, 0, st>>>(c->lay.n_params, c->w, c->w_inf, c->w16, c->w16_inf,
                                          c->cfg.path == NMG_PATH_FP16);
-  return check_launch("k_sync_copies");
+  NMG_TRY(check_launch("k_sync_copies"));
+  return pack_images(c, st);
 }
 
 }  // namespace nmg

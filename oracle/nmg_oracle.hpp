@@ -155,7 +155,9 @@ template <class S> inline V3<S> vmf_sample_local(S kappa, S u0, S u1) {
 // train.h:391-415 (tcnn/common_device.h:51 logistic).
 template <class S> inline S logistic(S x) { return S(1) / (S(1) + xexp(-x)); }
 template <class S> inline S act_exp(S x) { return xexp(std::min(std::max(x, S(-10)), S(15))); }
-template <class S> inline S act_softplus(S x) { return xlog(S(1) + xexp(x)); }
+// FP32 follows train.h:398 literally (log(1+e^x)); FP64 uses the stable form.
+inline float act_softplus(float x) { return logf(1.0f + expf(x)); }
+inline double act_softplus(double x) { return std::max(x, 0.0) + std::log1p(std::exp(-std::fabs(x))); }
 template <class S> inline S dact_softplus(S x) { S e = xexp(x); return e / (e + S(1)); }
 template <class S> inline S dact_logistic(S x) { S f = logistic(x); return f * (S(1) - f); }
 

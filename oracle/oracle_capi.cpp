@@ -311,7 +311,7 @@ static void matvec(const float* W, int rows, int cols, const double* x, double* 
 struct Fwd {
   double enc[256];
   double h[8][128];  // hidden activations after ReLU
-  double y[64];
+  double y[256];
 };
 
 static void forward_row(const nmgo_net* net, const GridSpec& g, const float* params, const float* x,

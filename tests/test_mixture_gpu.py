@@ -103,9 +103,11 @@ def test_loss_grad_vs_fp64(nmg, oracle, synth, K, selection, kappa_poly):
     scale = np.maximum(1.0, np.abs(g64[:, :nout]).max(axis=1))
     assert np.all(err <= 1e-3 * scale), err.max()
     assert np.all(g[:, nout:] == 0)
-    relL = np.abs(loss - l64) / np.maximum(np.abs(l64), 1e-6)
-    assert np.quantile(relL, 0.999) < 1e-5
-    assert abs(tot - t64) <= 1e-6 * abs(t64) + 1e-6
+    # loss = -(L/p) log q: its error is (L/p) dq/q, so the bound scales with L/p, not with the loss
+    wscale = ((rec[:, 2] + rec[:, 3] + rec[:, 4]) / 3.0) / (rec[:, 5] + 1e-5)
+    kmax = kappa_max(raw, K, False)
+    assert np.all(np.abs(loss - l64) <= wscale * (1e-5 + 4e-7 * kmax) + 1e-6 * np.abs(l64))
+    assert abs(tot - t64) <= 1e-5 * abs(t64) + 1e-6
 
 
 def test_loss_grad_golden_half_reference(nmg, golden):
@@ -117,10 +119,14 @@ def test_loss_grad_golden_half_reference(nmg, golden):
     g, loss, _ = nmg.mixture_loss_grad(r, rc, K, float(golden["loss_scale"]))
     g = g.cpu().numpy()[:, :4 * K]
     ref = golden["grad"][:, :4 * K]
-    tol = 2e-3 * np.abs(ref) + 1e-4 * np.maximum(1.0, np.abs(ref).max(axis=1, keepdims=True))
+    # __half storage (2^-11 relative) plus the FP32 conditioning of exp(kappa (cos - 1)) in both codes
+    kmax = kappa_max(golden["raw"], K, False)[:, None]
+    tol = (2e-3 + 8e-7 * kmax) * np.abs(ref) + 1e-4 * np.maximum(1.0, np.abs(ref).max(axis=1, keepdims=True))
     assert np.all(np.abs(g - ref) <= tol)
-    relL = np.abs(loss.cpu().numpy() - golden["loss"]) / np.maximum(np.abs(golden["loss"]), 1e-6)
-    assert relL.max() < 1e-4
+    rec = golden["rec"]
+    wscale = ((rec[:, 2] + rec[:, 3] + rec[:, 4]) / 3.0) / (rec[:, 5] + 1e-5)
+    errL = np.abs(loss.cpu().numpy() - golden["loss"])
+    assert np.all(errL <= wscale * (1e-4 + 8e-7 * kmax[:, 0]) + 1e-5 * np.abs(golden["loss"]))
     torch.cuda.synchronize()
 
 
@@ -142,8 +148,12 @@ def test_softplus_kappa(nmg, oracle, synth):
     r, u, rc = to_dev(raw, u4, rec)
     d, p, lb = nmg.mixture_sample(r, u, 8, kappa_softplus=True)
     d64, _, lb64 = oracle.mixture_sample(raw, 8, u4, fp64=True, o=oracle.opts(kappa_softplus=1))
-    ok = lb.cpu().numpy() == lb64
-    assert ok.mean() > 0.999
+    # a lobe whose kappa is within 1% of the 1e-5 switch to uniform sampling (vmf.h:49) may take either branch
+    kap = np.logaddexp(0.0, raw[:, 1:32:4].astype(np.float64))
+    lbg = lb.cpu().numpy()
+    near_switch = np.abs(kap[np.arange(len(lbg)), lbg] / 1e-5 - 1) < 1e-2
+    ok = (lbg == lb64) & ~near_switch
+    assert ok.mean() > 0.998
     assert np.abs(d.cpu().numpy()[ok] - d64[ok]).max() <= 1e-4
     g, _, _ = nmg.mixture_loss_grad(r, rc, 8, kappa_softplus=True)
     g64, _, _ = oracle.mixture_loss_grad(raw, 8, rec, fp64=True, o=oracle.opts(kappa_softplus=1))
