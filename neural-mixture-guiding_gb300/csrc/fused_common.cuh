@@ -1,0 +1,187 @@
+// fused_common.cuh -- device helpers shared by the fused query and training
+// kernels: the argument block, the row encoder that writes one input row
+// into a 16-bit operand tile in core-matrix order, and warpgroup barriers.
+#pragma once
+#include "ctx.cuh"
+#include "tcgen05.cuh"
+
+namespace nmg {
+
+constexpr int kWG = 4;          // warpgroups per CTA
+constexpr int kRows = 128;      // rows per tile (MMA M)
+
+struct FusedArgs {
+  EncodingParams enc;
+  MixOpts mix;
+  const uint8_t* wimg;               // packed weight image
+  uint32_t w_bytes;                  // image bytes (multiple of 16)
+  uint32_t layer_off[kMaxLayers];    // byte offset of each layer in the image
+  int n_layers;
+  int fp16;                          // operands FP16 instead of BF16
+  const uint16_t* table;             // 16-bit grid table [entries][F]
+  uint32_t lvl_T[kMaxLevels];        // entries per level
+  uint32_t lvl_hash;                 // bit l: level l is hashed (res^3 > T, T a power of two)
+  int raw_mode;                      // 1: inputs are network input rows x, output raw only
+  int n_out;                         // used outputs (4K [+1])
+  int n_out_pad;
+  int selection;
+  const float* pos;
+  const float* wo;
+  const float* nrm;
+  const float* rough;
+  const float* u4;
+  const float* x;
+  const int* d_count;
+  int n_max;
+  float* dir;
+  float* pdf;
+  int* lobe;
+  float* raw;
+  float* sel;
+  int* err;
+};
+
+NMG_D int fused_count(const int* d_count, int n_max) {
+  if (!d_count) return n_max;
+  int n = *d_count;
+  return n < 0 ? 0 : (n > n_max ? n_max : n);
+}
+
+NMG_D bool bar_red_and(int id, int count, bool v) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred pin, pout;\n\t"
+      "setp.ne.u32 pin, %1, 0;\n\t"
+      "bar.red.and.pred pout, %2, %3, pin;\n\t"
+      "selp.u32 %0, 1, 0, pout;\n\t}"
+      : "=r"(r)
+      : "r"(uint32_t(v)), "r"(id), "r"(count)
+      : "memory");
+  return r != 0;
+}
+
+NMG_D uint32_t level_index(const FusedArgs& a, int l, uint32_t x, uint32_t y, uint32_t z) {
+  const uint32_t T = a.lvl_T[l];
+  if ((a.lvl_hash >> l) & 1u) return (x ^ (y * 2654435761u) ^ (z * 805459861u)) & (T - 1u);
+  const uint32_t res = a.enc.res[l];
+  uint32_t idx = x + y * res + z * (res * res);
+  return idx < T ? idx : (idx < 2u * T ? idx - T : idx % T);
+}
+
+template <int BINS>
+NMG_D void oneblob_fixed(float x, float* o) {
+  const float nb = float(BINS);
+  float left = quartic_cdf(-x, nb) + quartic_cdf(-x - 1.f, nb) + quartic_cdf(-x + 1.f, nb);
+#pragma unroll
+  for (int k = 0; k < BINS; ++k) {
+    const float rb = float(k + 1) / nb;
+    float right = quartic_cdf(rb - x, nb) + quartic_cdf(rb - x - 1.f, nb) + quartic_cdf(rb - x + 1.f, nb);
+    o[k] = right - left;
+    left = right;
+  }
+}
+
+NMG_D void store_chunk(uint8_t* tile, int row, int chunk, int chunks, const float* f, bool fp16) {
+  uint4 v;
+  v.x = tc::pack2(f[0], f[1], fp16);
+  v.y = tc::pack2(f[2], f[3], fp16);
+  v.z = tc::pack2(f[4], f[5], fp16);
+  v.w = tc::pack2(f[6], f[7], fp16);
+  *reinterpret_cast<uint4*>(tile + tc::cm_offset(row, chunk, chunks)) = v;
+}
+
+template <int F>
+NMG_D void load_feats(const uint16_t* table, uint32_t entry, float* v, bool fp16) {
+  if (F == 2) {
+    uint32_t w = __ldg(reinterpret_cast<const uint32_t*>(table) + entry);
+    float2 p = tc::unpack2(w, fp16);
+    v[0] = p.x;
+    v[1] = p.y;
+  } else {
+    uint2 w = __ldg(reinterpret_cast<const uint2*>(table) + entry);
+    float2 p = tc::unpack2(w.x, fp16), q = tc::unpack2(w.y, fp16);
+    v[0] = p.x;
+    v[1] = p.y;
+    v[2] = q.x;
+    v[3] = q.y;
+  }
+}
+
+// Encodes one input row x into `tile` row `row` (KC 16-byte chunks).
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS>
+NMG_D void encode_row(const FusedArgs& a, const float* x, uint8_t* tile, int row) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NGRID = LEVELS * F;
+  constexpr int NPAD = (NGRID + NDIR + 15) / 16 * 16;
+  constexpr int KC = NPAD / 8;
+  constexpr int LPC = 8 / F;
+  static_assert(NGRID % 8 == 0, "grid features must fill whole chunks");
+  const bool fp16 = a.fp16 != 0;
+  const float p3[3] = {x[0], x[1], x[2]};
+#pragma unroll
+  for (int ch = 0; ch < NGRID / 8; ++ch) {
+    float f[8];
+#pragma unroll
+    for (int j = 0; j < LPC; ++j) {
+      const int l = ch * LPC + j;
+      float w[3];
+      uint32_t g[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[l], a.enc.smoothstep, &w[d], &g[d]);
+      float acc[F];
+#pragma unroll
+      for (int k = 0; k < F; ++k) acc[k] = 0.f;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const float wt = ((c & 1) ? w[0] : 1.f - w[0]) * ((c & 2) ? w[1] : 1.f - w[1]) * ((c & 4) ? w[2] : 1.f - w[2]);
+        const uint32_t e = a.enc.offset[l] +
+                           level_index(a, l, g[0] + (c & 1), g[1] + ((c >> 1) & 1), g[2] + ((c >> 2) & 1));
+        float v[F];
+        load_feats<F>(a.table, e, v, fp16);
+#pragma unroll
+        for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
+      }
+#pragma unroll
+      for (int k = 0; k < F; ++k) f[j * F + k] = acc[k];
+    }
+    store_chunk(tile, row, ch, KC, f, fp16);
+  }
+  float d[NPAD - NGRID];
+  sh_basis(SHDEG, x[3] * 2.f - 1.f, x[4] * 2.f - 1.f, x[5] * 2.f - 1.f, d);
+  if (MODE == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) oneblob_fixed<BINS>(x[6 + k], d + SHDEG * SHDEG + k * BINS);
+  } else {
+    sh_basis(SHDEG, x[6] * 2.f - 1.f, x[7] * 2.f - 1.f, x[8] * 2.f - 1.f, d + SHDEG * SHDEG);
+    oneblob_fixed<BINS>(x[9], d + 2 * SHDEG * SHDEG);
+  }
+#pragma unroll
+  for (int k = NDIR; k < NPAD - NGRID; ++k) d[k] = 1.f;
+#pragma unroll
+  for (int ch = 0; ch < (NPAD - NGRID) / 8; ++ch) store_chunk(tile, row, NGRID / 8 + ch, KC, d + 8 * ch, fp16);
+}
+
+NMG_D f3 face_fwd(f3 n, f3 v) { return dot3(n, v) > 0.f ? n : f3{-n.x, -n.y, -n.z}; }
+
+// ------------------------------------------------------------ weight image
+struct PackArgs {
+  long off[kMaxLayers + 1];
+  int in[kMaxLayers];
+  uint32_t layer_off[kMaxLayers];
+  int n_layers;
+};
+
+struct FusedState {
+  uint8_t* img_train;
+  uint8_t* img_infer;
+  int* err;
+  uint32_t w_bytes;
+  PackArgs pack;
+  int preset;  // 0 none, 1 hash-grid K8, 2 hash-grid K16, 3 reference K8
+};
+
+inline FusedState* fstate(nmg_ctx* c) { return reinterpret_cast<FusedState*>(c->ws.fused); }
+
+FusedArgs fused_make_args(nmg_ctx* c, bool infer_weights);
+
+}  // namespace nmg

@@ -168,12 +168,12 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
   f3 loc;
   float ph = NMG_TWO_PI * u1;
   float sp, cp;
-  if (k < NMG_EPS) {  // render/sampling.h:32-37
+  if (k < NMG_EPS) {  // render/sampling.h:32-37, then rotated like any lobe sample (vmf.h:67-71)
     float z = 1.f - 2.f * u0;
     float r = sqrtf(fmaxf(0.f, 1.f - z * z));
     xsincos<FAST>(ph, &sp, &cp);
-    return f3{r * cp, r * sp, z};
-  }
+    loc = f3{r * cp, r * sp, z};
+  } else {
   // cos(theta) = 1 + log1p(-u0 + e^{-2k} u0) / k (vmf.h:51), evaluated as
   // 1 - cos = -log1p(u0 expm1(-2k)) / k and, on the far hemisphere,
   // 1 + cos = log1p((1 - u0) expm1(2k)) / k, so that sin^2 = (1-cos)(1+cos)
@@ -192,6 +192,7 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
   float st = sqrtf(fmaxf(0.f, s2));
   xsincos<FAST>(ph, &sp, &cp);
   loc = f3{cp * st, sp * st, ct};
+  }
   // Frame(mu): T = normalize(mu x e), e the branchless axis pick; B = normalize(mu x T)
   float ax = fabsf(mu.x), ay = fabsf(mu.y), az = fabsf(mu.z);
   unsigned xm = ((ax - ay) < 0.f) & ((ax - az) < 0.f);
@@ -217,6 +218,16 @@ NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
   return p;
 }
 
+// Raw outputs of lobe i, from memory (16-byte aligned) or from registers.
+NMG_D float4 lobe4(const float* raw, int i) { return reinterpret_cast<const float4*>(raw)[i]; }
+template <int N>
+NMG_D float4 lobe4(const float (&raw)[N], int i) {
+  return make_float4(raw[4 * i], raw[4 * i + 1], raw[4 * i + 2], raw[4 * i + 3]);
+}
+NMG_D float raw_at(const float* raw, int i) { return raw[i]; }
+template <int N>
+NMG_D float raw_at(const float (&raw)[N], int i) { return raw[i < N ? i : 0]; }
+
 // Per-sample KL loss and gradient with respect to the raw outputs
 // (train.cu:69-124, distribution.h:144-181), FP32.
 //   raw: 4K raw outputs (16-byte aligned); rec: GuidedOutput {theta, phi,
@@ -224,13 +235,13 @@ NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
 // dF/dlambda uses the O(K) form (vmf_s - q)/total, algebraically equal to
 // the reference's O(K^2) sum. NaN/Inf gradients become 0 and gradients are
 // clamped above at 150 (train.cu:109-123). Returns the per-sample loss.
-template <int K, bool FAST>
-NMG_D float mix_kl_loss_grad(const float* raw, const float* rec, float scale, const MixOpts& o, float* grad) {
+template <int K, bool FAST, class RAW>
+NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, const MixOpts& o, float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
   float total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    float4 r = reinterpret_cast<const float4*>(raw)[i];
+    float4 r = lobe4(raw, i);
     lam[i] = xexp<FAST>(act_exp_clamp(r.x));
     if (o.kappa_softplus) {
       kap[i] = softplus<FAST>(r.y);
@@ -301,14 +312,14 @@ NMG_D float mix_kl_loss_grad(const float* raw, const float* rec, float scale, co
 // train.cu:126-172: the learned-selection variant. raw[4K] is the selection
 // logit; rec[6] the BSDF pdf of the direction. No NaN/clamp post-pass
 // (the reference has none for this variant). grad has 4K+1 entries.
-template <int K, bool FAST>
-NMG_D float mix_kl_loss_grad_selection(const float* raw, const float* rec, float scale, const MixOpts& o,
+template <int K, bool FAST, class RAW>
+NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float scale, const MixOpts& o,
                                        float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
   float total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    float4 r = reinterpret_cast<const float4*>(raw)[i];
+    float4 r = lobe4(raw, i);
     lam[i] = xexp<FAST>(act_exp_clamp(r.x));
     if (o.kappa_softplus) {
       kap[i] = softplus<FAST>(r.y);
@@ -323,7 +334,7 @@ NMG_D float mix_kl_loss_grad_selection(const float* raw, const float* rec, float
     xsincos<FAST>(NMG_TWO_PI * sgp[i], &sph[i], &cph[i]);
     total += lam[i];
   }
-  const float xs = raw[4 * K];
+  const float xs = raw_at(raw, 4 * K);
   const float sel = logistic<FAST>(xs);
   float swt, cwt, swp, cwp;
   xsincos<FAST>(rec[0], &swt, &cwt);

@@ -156,7 +156,7 @@ static nmg_status reserve(nmg_ctx* c, int max_q, int max_b) {
   A(w.partials, 2 * 2048);
   A(w.raw, capz * L.n_out_pad);
   w.n_partials = 2 * 2048;
-  if (c->cfg.path == NMG_PATH_FP32) {
+  if (c->cfg.path == NMG_PATH_FP32 || max_b > 0) {
     A(w.enc, capz * c->enc.n_enc_pad);
     for (int l = 0; l < L.n_layers - 1; ++l)
       if (l < 2 || max_b > 0) A(w.h[l], capz * kWidth);

@@ -57,6 +57,7 @@ def lib():
         L.nmgo_featurize.argtypes = [C.POINTER(Net), C.c_long, P, P, P, P, P, P]
         L.nmgo_network_forward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P]
         L.nmgo_network_backward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P, P]
+        L.nmgo_grid_backward.argtypes = [C.POINTER(Net), C.c_long, P, P, P]
         L.nmgo_adam_ema.argtypes = [C.c_long, C.c_long, P, C.c_float, C.c_float, C.c_float, C.c_float,
                                     C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P, P]
         _lib = L
@@ -150,6 +151,15 @@ def network_backward(net, params, inputs, draw, want_denc=False):
     denc = np.zeros((n, net.n_enc_padded), np.float64) if want_denc else None
     lib().nmgo_network_backward(C.byref(net), _p(params), n, _p(inputs), _p(draw), _p(dparams), _p(denc))
     return (dparams, denc) if want_denc else dparams
+
+
+def grid_backward(net, inputs, denc):
+    """Table gradient (FP64) from dL/d(encoded input) rows."""
+    inputs = _f32(inputs)
+    denc = np.ascontiguousarray(denc, np.float64)
+    out = np.zeros(net.n_grid_params, np.float64)
+    lib().nmgo_grid_backward(C.byref(net), inputs.shape[0], _p(inputs), _p(denc), _p(out))
+    return out
 
 
 def adam_ema(grad, loss_scale, lr, beta1, beta2, eps, l2, ema_decay, step, w, m, v, psteps, ema, n_matrix):

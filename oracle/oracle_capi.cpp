@@ -472,3 +472,10 @@ extern "C" void nmgo_adam_ema(long n_params, long n_matrix, const float* grad, f
   }
 }
 
+// Grid part of the backward only: dL/d(encoded input) rows denc[n x
+// n_enc_padded] (FP64) -> table gradient (accumulated into dgrid).
+extern "C" void nmgo_grid_backward(const nmgo_net* net, long n, const float* inputs, const double* denc, double* dgrid) {
+  GridSpec g = grid_of(net);
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < n; ++i) grid_backward_atomic(g, inputs + i * net->n_input, denc + i * net->n_enc_padded, dgrid);
+}

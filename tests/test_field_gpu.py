@@ -135,11 +135,13 @@ def test_vjp_matches_oracle(field, oracle, synth):
     block_close(dp.cpu().numpy(), dp64, net)
 
 
-def test_train_step_gradient_and_adam(field, oracle, synth):
+@pytest.mark.parametrize("n", [4096, 40000], ids=["small", "multi-block"])
+def test_train_step_gradient_and_adam(field, oracle, synth, n):
     f, net = field
     K, sel = f.cfg.n_lobes, bool(f.cfg.selection)
+    f.reserve(0, n)
     fieldgt = synth.TrainField(seed=1)
-    x, rec = synth.train_batch(fieldgt, 4096, seed=2, input_mode=f.cfg.input_mode, selection=sel)
+    x, rec = synth.train_batch(fieldgt, n, seed=2, input_mode=f.cfg.input_mode, selection=sel)
     w0 = f.get_params(0).cpu().numpy()
     stats = f.train_step(*dev(x, rec)).cpu().numpy()
     g = f.get_gradients().cpu().numpy()
@@ -148,7 +150,7 @@ def test_train_step_gradient_and_adam(field, oracle, synth):
     graw, loss, tot = oracle.mixture_loss_grad(raw64.astype(np.float32), K, rec, 128.0, selection=sel, fp64=True)
     g64 = oracle.network_backward(net, w0, x, graw)
     block_close(g, g64, net, tol=2e-3)
-    assert abs(stats[0] - tot / 4096) <= 1e-4 * abs(tot / 4096)
+    assert abs(stats[0] - tot / n) <= 1e-4 * abs(tot / n)
     assert abs(stats[1] - np.linalg.norm(g.astype(np.float64) / 128.0)) <= 1e-6 * stats[1]
     # Adam + EMA applied by the oracle to the GPU's own gradient
     w, m, v = w0.copy(), np.zeros_like(w0), np.zeros_like(w0)

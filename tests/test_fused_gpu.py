@@ -112,3 +112,110 @@ def test_fused_device_count_and_ragged(field, synth):
         assert bool((out["pdf"][c:] == -1).all())
     f.L.nmg_check_errors.argtypes = [__import__("ctypes").c_void_p]
     assert f.L.nmg_check_errors(f.h) == 0
+
+
+def block_errors(g, g64, net):
+    offs = [0]
+    w_in = net.n_enc_padded
+    for _ in range(net.n_hidden):
+        offs.append(offs[-1] + net.width * w_in)
+        w_in = net.width
+    offs.append(offs[-1] + net.n_out_padded * net.width)
+    offs.append(net.n_params)
+    out = []
+    for a, b in zip(offs[:-1], offs[1:]):
+        ref, got = g64[a:b], g[a:b]
+        out.append((np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-30),
+                    np.sqrt(((got - ref) ** 2).mean()) / max(np.sqrt((ref ** 2).mean()), 1e-30)))
+    return out
+
+
+def split_mlp(net, w):
+    """Weight matrices (row-major [out][in]) of a parameter vector."""
+    mats, off, w_in = [], 0, net.n_enc_padded
+    for _ in range(net.n_hidden):
+        mats.append(w[off:off + net.width * w_in].reshape(net.width, w_in))
+        off += net.width * w_in
+        w_in = net.width
+    mats.append(w[off:off + net.n_out_padded * net.width].reshape(net.n_out_padded, net.width))
+    return mats
+
+
+def emulate_fused_gradient(oracle, net, w16, x, rec, K, sel, fp16):
+    """The fused training kernel's arithmetic on the host: FP64 products with 16-bit rounding exactly
+    where the kernel stores a 16-bit operand tile (encoded inputs, hidden activations, deltas), the
+    adjoint from the FP64 oracle, and the delta range factor S (n for BF16, min(n, 256) for FP16)."""
+    import torch
+    dt = torch.float16 if fp16 else torch.bfloat16
+
+    def rnd(t):
+        return t.to(dt).to(torch.float64)
+
+    n = x.shape[0]
+    S = float(min(n, 256) if fp16 else n)
+    _, enc = oracle.network_forward(net, w16, x, want_enc=True)
+    W = [torch.from_numpy(m.astype(np.float64)) for m in split_mlp(net, w16)]
+    a0 = rnd(torch.from_numpy(enc))
+    h0 = rnd(torch.relu(a0 @ W[0].T))
+    h1 = rnd(torch.relu(h0 @ W[1].T))
+    h2 = rnd(torch.relu(h1 @ W[2].T))
+    raw = (h2 @ W[3].T).numpy()
+    g, _, tot = oracle.mixture_loss_grad(raw.astype(np.float32), K, rec, 128.0, selection=sel, fp64=True)
+    d3 = rnd(torch.from_numpy(g) * S)
+    dW3 = d3.T @ h2
+    d2 = rnd((d3 @ W[3]) * (h2 > 0))
+    dW2 = d2.T @ h1
+    d1 = rnd((d2 @ W[2]) * (h1 > 0))
+    dW1 = d1.T @ h0
+    d0 = rnd((d1 @ W[1]) * (h0 > 0))
+    dW0 = d0.T @ a0
+    denc = (d0 @ W[0]).numpy()
+    grid = oracle.grid_backward(net, x, denc)
+    mlp = np.concatenate([m.numpy().ravel() for m in (dW0, dW1, dW2, dW3)])
+    return np.concatenate([mlp, grid]) / S, tot
+
+
+@pytest.mark.parametrize("n", [4096, 40000], ids=["one-tile-per-cta", "multi-tile"])
+def test_fused_train_gradient(field, oracle, synth, n):
+    """One fused training step: the loss-scaled gradient against the host emulation of the same 16-bit
+    rounding points (tight), and against the FP64 oracle on the same 16-bit weights (loose, the
+    precision cost of 16-bit activations). 40,000 records give every CTA more than one tile, so the
+    TMEM weight-gradient accumulation across tiles is exercised."""
+    f, net, fp16 = field
+    perturb(f, 3)
+    K, sel = f.cfg.n_lobes, bool(f.cfg.selection)
+    f.reserve(0, n)
+    gt = synth.TrainField(seed=5)
+    x, rec = synth.train_batch(gt, n, seed=6, input_mode=f.cfg.input_mode, selection=sel)
+    w16 = round16(f.get_params(0).cpu().numpy(), fp16)
+    stats = f.train_step(*dev(x, rec)).cpu().numpy()
+    g = f.get_gradients().cpu().numpy()
+    g_emu, tot = emulate_fused_gradient(oracle, net, w16, x, rec, K, sel, fp16)
+    errs = block_errors(g, g_emu, net)
+    for i, (emax, erms) in enumerate(errs):
+        assert erms <= 5e-3 and emax <= 5e-2, ("emulation", i, emax, erms)
+    raw64 = oracle.network_forward(net, w16, x)
+    graw, _, tot64 = oracle.mixture_loss_grad(raw64.astype(np.float32), K, rec, 128.0, selection=sel, fp64=True)
+    g64 = oracle.network_backward(net, w16, x, graw)
+    for i, (emax, erms) in enumerate(block_errors(g, g64, net)):
+        assert erms <= (0.02 if fp16 else 0.10), ("fp64", i, emax, erms)
+    assert abs(stats[0] - tot64 / n) <= 2e-2 * abs(tot64 / n)
+    assert f.step == 1
+    f.L.nmg_check_errors.argtypes = [__import__("ctypes").c_void_p]
+    assert f.L.nmg_check_errors(f.h) == 0
+
+
+def test_fused_train_large_batch_and_ragged(field, synth):
+    """Batches that are not a multiple of the 128-row tile and larger than one tile per SM run
+    without error, and the device count clamps the batch."""
+    import torch
+    f, net, fp16 = field
+    gt = synth.TrainField(seed=7)
+    x, rec = synth.train_batch(gt, 4000, seed=8, input_mode=f.cfg.input_mode, selection=bool(f.cfg.selection))
+    xd, rd = dev(x, rec)
+    s1 = f.train_step(xd, rd).cpu().numpy()
+    cnt = torch.tensor([1234], dtype=torch.int32, device="cuda")
+    s2 = f.train_step(xd, rd, count=cnt).cpu().numpy()
+    assert np.all(np.isfinite(s1)) and np.all(np.isfinite(s2))
+    f.L.nmg_check_errors.argtypes = [__import__("ctypes").c_void_p]
+    assert f.L.nmg_check_errors(f.h) == 0

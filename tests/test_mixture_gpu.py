@@ -103,31 +103,46 @@ def test_loss_grad_vs_fp64(nmg, oracle, synth, K, selection, kappa_poly):
     scale = np.maximum(1.0, np.abs(g64[:, :nout]).max(axis=1))
     assert np.all(err <= 1e-3 * scale), err.max()
     assert np.all(g[:, nout:] == 0)
-    # loss = -(L/p) log q: its error is (L/p) dq/q, so the bound scales with L/p, not with the loss
-    wscale = ((rec[:, 2] + rec[:, 3] + rec[:, 4]) / 3.0) / (rec[:, 5] + 1e-5)
+    # loss = -(L/p) log q: its error is (L/p) dq/q (and, with learned selection where p is the model's
+    # own pdf, (L/p)(1 + |log p|) dp/p), so the bound scales with L/p, not with the loss itself
+    Li = (rec[:, 2] + rec[:, 3] + rec[:, 4]) / 3.0
+    if selection:
+        wi = np.stack([np.sin(rec[:, 0]) * np.cos(rec[:, 1]), np.sin(rec[:, 0]) * np.sin(rec[:, 1]),
+                       np.cos(rec[:, 0])], axis=1)
+        q64 = oracle.mixture_pdf(raw, K, wi, fp64=True)
+        sel = 1.0 / (1.0 + np.exp(-raw[:, 4 * K].astype(np.float64)))
+        p = sel * (q64 + 1e-5) + (1 - sel) * rec[:, 6]
+        wscale = Li / p * (1.0 + np.abs(np.log(p)))
+    else:
+        wscale = Li / (rec[:, 5] + 1e-5)
     kmax = kappa_max(raw, K, False)
     assert np.all(np.abs(loss - l64) <= wscale * (1e-5 + 4e-7 * kmax) + 1e-6 * np.abs(l64))
     assert abs(tot - t64) <= 1e-5 * abs(t64) + 1e-6
 
 
-def test_loss_grad_golden_half_reference(nmg, golden):
-    """GPU FP32 gradient against the reference's __half-stored gradient."""
-    import torch
+def test_loss_grad_golden_half_reference(nmg, oracle, golden):
+    """GPU FP32 gradient against the reference's __half-stored gradient.
+
+    The reference rounds the mixture gradient to __half before and after the
+    chain-rule products (train.cu:91-103); that rounding is the measured
+    difference between the golden values and the FP64 oracle, and the GPU's
+    FP32 result must lie within it (plus FP32 conditioning)."""
     K = int(golden["K"])
     raw_h = golden["raw"].astype(np.float16).astype(np.float32)
     r, rc = to_dev(raw_h, golden["rec"])
     g, loss, _ = nmg.mixture_loss_grad(r, rc, K, float(golden["loss_scale"]))
     g = g.cpu().numpy()[:, :4 * K]
     ref = golden["grad"][:, :4 * K]
-    # __half storage (2^-11 relative) plus the FP32 conditioning of exp(kappa (cos - 1)) in both codes
-    kmax = kappa_max(golden["raw"], K, False)[:, None]
-    tol = (2e-3 + 8e-7 * kmax) * np.abs(ref) + 1e-4 * np.maximum(1.0, np.abs(ref).max(axis=1, keepdims=True))
+    g64, l64, _ = oracle.mixture_loss_grad(raw_h, K, golden["rec"], float(golden["loss_scale"]), fp64=True)
+    g64 = g64[:, :4 * K]
+    kmax = kappa_max(raw_h, K, False)[:, None]
+    # FP32 error of dF/dlambda = (vmf_s - q)/total scales with the row's largest terms (cancellation)
+    tol = np.abs(ref - g64) * 1.01 + (2e-5 + 8e-7 * kmax) * np.abs(g64).max(axis=1, keepdims=True)
     assert np.all(np.abs(g - ref) <= tol)
     rec = golden["rec"]
     wscale = ((rec[:, 2] + rec[:, 3] + rec[:, 4]) / 3.0) / (rec[:, 5] + 1e-5)
     errL = np.abs(loss.cpu().numpy() - golden["loss"])
-    assert np.all(errL <= wscale * (1e-4 + 8e-7 * kmax[:, 0]) + 1e-5 * np.abs(golden["loss"]))
-    torch.cuda.synchronize()
+    assert np.all(errL <= np.abs(golden["loss"] - l64) * 1.01 + wscale * (1e-5 + 8e-7 * kmax[:, 0]) + 1e-6)
 
 
 def test_empty_and_ragged_batches(nmg, oracle, synth):
