@@ -95,7 +95,6 @@ template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
 __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant__ TrainArgs ta) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
-  constexpr int KC0 = NENC / 8;
   constexpr uint32_t A_BYTES = kRows * NENC * 2;
   constexpr uint32_t H_BYTES = kRows * kWidth * 2;
   constexpr uint32_t D_BYTES = kRows * (NOUTMAX > kWidth ? NOUTMAX : kWidth) * 2;  // delta tile (output width)
