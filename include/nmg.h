@@ -111,6 +111,25 @@ nmg_status nmg_mixture_loss_grad(const nmg_mixture_opts* opts, const float* raw,
                                  nmg_stream stream);
 
 
+/*
+ * nmg_mixture_loss_grad without a caller-provided workspace. This entry point
+ * has no counterpart in the reference; it exists for callers that cannot
+ * allocate device memory (all of it pooled before the frame loop, no
+ * allocator handle of their own, or no tolerance for the synchronisation a
+ * cudaMalloc/cudaFree may cause). It allocates nothing: the FP64 loss sum is
+ * reduced through a fixed 64 KiB array inside libnmg.so that every GPU
+ * loading the library keeps until the process exits, which limits n to
+ * 1,048,576 samples (larger n returns NMG_ERR_CAPACITY). The first call on
+ * each device looks up that array's device address; make that first call
+ * before any stream capture. All calls share the array: calls that overlap
+ * on the GPU (different streams, or different host threads) race on it and
+ * must be ordered by the caller. Results equal nmg_mixture_loss_grad's
+ * (loss_sum up to the order of the FP64 additions).
+ */
+nmg_status nmg_mixture_loss_grad_noalloc(const nmg_mixture_opts* opts, const float* raw, const float* record,
+                                         int record_stride, int n, float loss_scale, float* grad, float* loss,
+                                         double* loss_sum, nmg_stream stream);
+
 /* ------------------------------------------------------------------------
  * Network-backed guiding field (encoding -> MLP -> mixture).
  * ---------------------------------------------------------------------- */

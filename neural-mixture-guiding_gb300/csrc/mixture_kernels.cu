@@ -8,6 +8,8 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
+
 #include "api_common.cuh"
 #include "mixture.cuh"
 
@@ -254,3 +256,98 @@ nmg_status nmg_mixture_loss_grad(const nmg_mixture_opts* opts, const float* raw,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of nmg_mixture_loss_grad.
+//
+// Some callers of this library cannot hand it a scratch buffer: a renderer
+// whose device memory is entirely carved into pools before the frame loop
+// starts, a plugin that only ever receives raw pointers from its host and has
+// no allocator of its own, or a real-time loop that cannot afford the
+// device-wide synchronisation a cudaMalloc/cudaFree may cause in the middle
+// of a frame. For them the FP64 loss reduction keeps its per-block partial
+// sums in the fixed array below, which lives in this library's own device
+// image: every GPU that loads the library holds these 64 KiB until the
+// process exits. One slot per 128-sample block gives a limit of
+// kNoAllocMaxSamples samples per call.
+// ---------------------------------------------------------------------------
+namespace nmg {
+constexpr int kNoAllocSlots = 8192;                          // 64 KiB of FP64 partial sums
+constexpr int kNoAllocMaxSamples = kNoAllocSlots * kThreads;  // 1,048,576 samples per call
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocSlots];
+
+// Device address of g_noalloc_partials per device, looked up once per device
+// (the symbol's host-side name is not a device address).
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[128] = {};
+
+static nmg_status noalloc_scratch(double** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 128) return set_error(NMG_ERR_UNSUPPORTED, "device ordinal %d above 127", dev);
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess)
+      return set_error(NMG_ERR_CUDA, "cudaGetSymbolAddress(loss scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return NMG_OK;
+}
+
+template <int K>
+static nmg_status launch_loss_noalloc(const nmg_mixture_opts* o, const float* raw, const float* rec, int rstride,
+                                      int n, float loss_scale, float* grad, float* loss, double* loss_sum,
+                                      double* partials, cudaStream_t st) {
+  MixOpts mo{o->kappa_softplus, o->kappa_poly, 0};
+  const int blocks = (n + kThreads - 1) / kThreads;  // one partial per block, every slot rewritten
+  const float scale = loss_scale / float(n);
+  if (o->selection)
+    k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
+                                                              loss_sum ? partials : nullptr);
+  else
+    k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
+                                                               loss_sum ? partials : nullptr);
+  nmg_status s = check_launch("nmg_mixture_loss_grad_noalloc");
+  if (s != NMG_OK || !loss_sum) return s;
+  k_sum_partials<<<1, 256, 0, st>>>(partials, blocks, loss_sum);
+  return check_launch("nmg_mixture_loss_grad_noalloc (sum)");
+}
+}  // namespace nmg
+
+extern "C" nmg_status nmg_mixture_loss_grad_noalloc(const nmg_mixture_opts* opts, const float* raw,
+                                                    const float* record, int record_stride, int n, float loss_scale,
+                                                    float* grad, float* loss, double* loss_sum, nmg_stream stream) {
+  nmg_status s = check_opts(opts);
+  if (s != NMG_OK) return s;
+  NMG_REQUIRE(n >= 0, "n=%d < 0", n);
+  if (n > kNoAllocMaxSamples)
+    return set_error(NMG_ERR_CAPACITY,
+                     "n=%d above the %d-sample limit of nmg_mixture_loss_grad_noalloc (its fixed scratch holds "
+                     "%d block sums); use nmg_mixture_loss_grad with a workspace",
+                     n, kNoAllocMaxSamples, kNoAllocSlots);
+  NMG_REQUIRE(record_stride >= (opts->selection ? 7 : 6) && record_stride <= 8,
+              "record_stride=%d: GuidedOutput rows have 6 floats (7 with selection), at most 8", record_stride);
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    if (loss_sum) NMG_CUDA_TRY(cudaMemsetAsync(loss_sum, 0, sizeof(double), st));
+    return NMG_OK;
+  }
+  NMG_REQUIRE(raw && record && grad, "raw, record and grad must be non-NULL");
+  NMG_REQUIRE(aligned16(raw) && aligned16(grad), "raw and grad must be 16-byte aligned");
+  double* partials = nullptr;
+  if (loss_sum) {
+    s = noalloc_scratch(&partials);
+    if (s != NMG_OK) return s;
+  }
+  switch (opts->n_lobes) {
+    case 4: return launch_loss_noalloc<4>(opts, raw, record, record_stride, n, loss_scale, grad, loss, loss_sum, partials, st);
+    case 7: return launch_loss_noalloc<7>(opts, raw, record, record_stride, n, loss_scale, grad, loss, loss_sum, partials, st);
+    case 8: return launch_loss_noalloc<8>(opts, raw, record, record_stride, n, loss_scale, grad, loss, loss_sum, partials, st);
+    case 16: return launch_loss_noalloc<16>(opts, raw, record, record_stride, n, loss_scale, grad, loss, loss_sum, partials, st);
+  }
+  return NMG_ERR_UNSUPPORTED;
+}
