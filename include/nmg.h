@@ -298,6 +298,25 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
 nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int n, float* raw, float* dparams,
                            nmg_stream stream);
 
+/*
+ * Tiling of the fused query kernel: warpgroups (128-query tiles in flight)
+ * per CTA, one CTA per SM; 0 selects the default (4). 5 and 6 are valid when
+ * the padded output width is <= 64. No counterpart in the reference (its
+ * FullyFusedMLP launch shape is fixed, fully_fused_mlp.cu:500-558).
+ */
+nmg_status nmg_set_query_tiling(nmg_ctx* ctx, int warpgroups_per_cta);
+int nmg_get_query_tiling(const nmg_ctx* ctx);
+
+/*
+ * Autotuner: times the fused query kernel on the caller's inputs for every
+ * candidate tiling (outputs are overwritten), keeps the fastest for this
+ * context and reports it in *chosen. With use_cache the choice is read from /
+ * appended to a text cache ($NMG_TUNE_CACHE, default ~/.cache/nmg_tune.txt)
+ * keyed by device, configuration and log2 of n. Synchronises the stream.
+ */
+nmg_status nmg_autotune_query(nmg_ctx* ctx, const nmg_shading* in, const float* u4, int n,
+                              const nmg_query_out* out, int use_cache, int* chosen, nmg_stream stream);
+
 /* Synchronises the device and reports an error recorded by a kernel of this
  * context since the last check (NMG_ERR_TIMEOUT when a bounded device wait
  * gave up). */

@@ -172,6 +172,9 @@ def _bind_field(L):
         "nmg_pdf": [P, C.POINTER(Shading), P, P, C.c_int, P, P],
         "nmg_train_step": [P, P, P, P, C.c_int, P, P],
         "nmg_network_vjp": [P, P, P, C.c_int, P, P, P],
+        "nmg_set_query_tiling": [P, C.c_int],
+        "nmg_autotune_query": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), C.c_int, C.POINTER(C.c_int), P],
+        "nmg_check_errors": [P],
         "nmg_save": [P, C.c_char_p],
         "nmg_load": [P, C.c_char_p],
     }
@@ -183,6 +186,8 @@ def _bind_field(L):
     L.nmg_destroy.restype = None
     L.nmg_get_step.argtypes = [P]
     L.nmg_get_step.restype = C.c_int
+    L.nmg_get_query_tiling.argtypes = [P]
+    L.nmg_get_query_tiling.restype = C.c_int
 
 
 def config(preset=PRESET_HASHGRID, **overrides):
@@ -324,6 +329,28 @@ class GuidingField:
             dparams = torch.zeros(self.n_params, device="cuda")
         check(self.L.nmg_network_vjp(self.h, _ptr(x), _ptr(draw), n, _ptr(raw), _ptr(dparams), _stream(stream)))
         return raw, dparams
+
+    def set_query_tiling(self, warpgroups_per_cta):
+        check(self.L.nmg_set_query_tiling(self.h, int(warpgroups_per_cta)))
+
+    @property
+    def query_tiling(self):
+        return self.L.nmg_get_query_tiling(self.h)
+
+    def autotune(self, pos, wo, normal, rough, u4, use_cache=False, stream=None):
+        """Picks the fastest fused-query tiling on these inputs; returns it."""
+        import torch
+        n = pos.shape[0]
+        out = {"dir": torch.empty((n, 3), device="cuda"), "pdf": torch.empty(n, device="cuda")}
+        o = QueryOut(out["dir"].data_ptr(), out["pdf"].data_ptr(), None, None, None)
+        sh = self.shading(pos, wo, normal, rough)
+        chosen = C.c_int(0)
+        check(self.L.nmg_autotune_query(self.h, C.byref(sh), _ptr(u4), n, C.byref(o), int(use_cache),
+                                        C.byref(chosen), _stream(stream)))
+        return chosen.value
+
+    def check_errors(self):
+        check(self.L.nmg_check_errors(self.h))
 
     def save(self, path):
         check(self.L.nmg_save(self.h, path.encode()))

@@ -5,6 +5,10 @@
 #include <stdarg.h>
 #include <stdio.h>
 
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "../../include/nmg.h"
 
 namespace nmg {
@@ -19,6 +23,38 @@ inline nmg_status check_launch(const char* what) {
 }
 
 inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+// Raises a kernel's dynamic shared-memory limit to at least `bytes`, once per
+// (kernel, device): launches inside a stream capture then make no attribute
+// calls.
+inline nmg_status ensure_smem(const void* kern, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, size_t> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& have = done[{kern, dev}];
+  if (have >= bytes) return NMG_OK;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "shared memory %zu B: %s", bytes, cudaGetErrorString(e));
+  have = bytes;
+  return NMG_OK;
+}
+
+// Number of SMs of the current device (looked up once per device).
+inline int sm_count() {
+  static std::mutex mu;
+  static std::map<int, int> cache;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = cache.find(dev);
+  if (it != cache.end()) return it->second;
+  int n = 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  cache[dev] = n;
+  return n;
+}
 
 }  // namespace nmg
 

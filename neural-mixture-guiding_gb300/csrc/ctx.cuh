@@ -58,6 +58,7 @@ struct nmg_ctx {
   // reduced-precision copies for the fused path (bf16 or fp16 bits)
   uint16_t* w16 = nullptr;     // training weights
   uint16_t* w16_inf = nullptr; // inference weights
+  int query_wg = 0;            // warpgroups per CTA of the fused query kernel (0: default)
   nmg::Workspace ws;
 };
 
@@ -91,6 +92,8 @@ nmg_status fused_infer_raw(nmg_ctx* c, const float* x, const int* d_count, int n
 nmg_status pack_images(nmg_ctx* c, cudaStream_t st);
 void fused_release(nmg_ctx* c);
 nmg_status fused_check_errors(nmg_ctx* c);
+nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
+                          int use_cache, int* chosen, cudaStream_t st);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st);
 

@@ -21,7 +21,11 @@
 // distribution.h / vmf.h) up to the BF16/FP16 rounding of features,
 // weights and activations, and fast-math transcendental functions.
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
+#include <sys/stat.h>
+
+#include <string>
 
 #include "api_common.cuh"
 #include "ctx.cuh"
@@ -30,29 +34,31 @@
 
 namespace nmg {
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
-__global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_constant__ FusedArgs a) {
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
+__global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_constant__ FusedArgs a) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
-  constexpr uint32_t A_BYTES = kRows * NENC * 2;
-  constexpr uint32_t H_BYTES = kRows * kWidth * 2;
+  // One operand tile per warpgroup: the encoded inputs, then (once the first
+  // layer's MMA has read them) the hidden activations of every later layer.
+  constexpr uint32_t TILE_BYTES = kRows * (NENC > kWidth ? NENC : kWidth) * 2;
   constexpr uint32_t COLS = NOUTMAX <= 64 ? 64 : 128;  // TMEM columns per warpgroup
+  constexpr uint32_t TCOLS = COLS * NWG <= 256 ? (COLS * NWG <= 128 ? 128 : 256) : 512;
+  static_assert(COLS * NWG <= 512, "TMEM holds 512 columns");
   extern __shared__ __align__(1024) uint8_t smem[];
 
   const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
   const int wg = threadIdx.x / kRows, t = threadIdx.x % kRows, warp_in_wg = t / 32;
   uint8_t* wsm = smem;
-  uint8_t* A = smem + w_region + wg * (A_BYTES + H_BYTES);
-  uint8_t* H = A + A_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + kWG * (A_BYTES + H_BYTES));
+  uint8_t* A = smem + w_region + wg * TILE_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * TILE_BYTES);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 8);
 
   if (threadIdx.x == 0) {
     tc::mbar_init(&bars[0], 1);
-    for (int g = 0; g < kWG; ++g) tc::mbar_init(&bars[1 + g], 1);
+    for (int g = 0; g < NWG; ++g) tc::mbar_init(&bars[1 + g], 1);
     tc::fence_mbar_init();
   }
-  if (threadIdx.x < 32) tc::tmem_alloc(tslot, COLS * kWG);
+  if (threadIdx.x < 32) tc::tmem_alloc(tslot, TCOLS);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
@@ -75,30 +81,30 @@ __global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_con
   const int n = fused_count(a.d_count, a.n_max);
   const int ntiles = (n + kRows - 1) / kRows;
   const int nl = a.n_layers;
+  const uint32_t a_addr = tc::smem_u32(A);
 
   // Every early exit below follows a warpgroup-wide bar.red.and, so the 128
   // threads of a group always leave the loop together (no thread can be
   // left waiting at a named barrier).
-  for (int tile = blockIdx.x * kWG + wg; tile < ntiles; tile += gridDim.x * kWG) {
+  for (int tile = blockIdx.x * NWG + wg; tile < ntiles; tile += gridDim.x * NWG) {
     const long q = long(tile) * kRows + t;
     const bool valid = q < n;
-    // ---- encode this thread's row into A
+    // ---- encode this thread's row into the tile
     float x[10];
 #pragma unroll
     for (int d = 0; d < 10; ++d) x[d] = 0.f;
     if (valid) {
-      if (a.raw_mode) {
-        for (int d = 0; d < a.enc.n_input; ++d) x[d] = a.x[q * a.enc.n_input + d];
-      } else {
+      if (a.raw_mode)
+        load_row(a.x, q, a.enc.n_input, x);
+      else
         featurize(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
-      }
     }
-    encode_row<F, LEVELS, MODE, SHDEG, BINS>(a, x, A, t);
+    encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH>(a, x, A, t);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     ok = bar_red_and(1 + wg, kRows, ok);
     if (!ok) break;
-    // ---- MLP: layer l reads A (l == 0) or H, writes TMEM; hidden layers go back to H
+    // ---- MLP: every layer reads the tile and writes TMEM; hidden layers write the tile back
     float r[NOUTMAX];
     bool last_ok = true;
     for (int l = 0; l < nl; ++l) {
@@ -107,7 +113,6 @@ __global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_con
       const int nout = last ? a.n_out_pad : kWidth;
       if (t == 0) {
         tc::fence_after_sync();
-        const uint32_t a_addr = tc::smem_u32(l == 0 ? A : H);
         const uint32_t b_addr = tc::smem_u32(wsm) + a.layer_off[l];
         const uint32_t sbo = uint32_t(kin / 8) * 128u;
         const uint32_t idesc = tc::idesc_f16(kRows, nout, fp16);
@@ -129,7 +134,7 @@ __global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_con
           float f[8];
 #pragma unroll
           for (int i = 0; i < 8; ++i) f[i] = fmaxf(v[8 * c + i], 0.f);
-          store_chunk(H, t, c, kWidth / 8, f, fp16);
+          store_chunk(A, t, c, kWidth / 8, f, fp16);
         }
         tc::fence_proxy_async();
         tc::fence_before_sync();
@@ -172,7 +177,7 @@ __global__ void __launch_bounds__(kWG * kRows, 1) k_fused_query(const __grid_con
   __syncthreads();
   if (threadIdx.x < 32) {
     tc::fence_after_sync();
-    tc::tmem_dealloc(*tslot, COLS * kWG);
+    tc::tmem_dealloc(*tslot, TCOLS);
   }
 }
 
@@ -206,34 +211,46 @@ static int preset_of(const nmg_ctx* c) {
   return 0;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int NWG>
 static size_t smem_bytes_for(uint32_t w_bytes) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
-  return size_t((w_bytes + 1023u) & ~1023u) + kWG * (size_t(kRows) * NENC * 2 + size_t(kRows) * kWidth * 2) + 128;
+  return size_t((w_bytes + 1023u) & ~1023u) + NWG * size_t(kRows) * (NENC > kWidth ? NENC : kWidth) * 2 + 128;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
-static nmg_status launch_query(const FusedArgs& a, cudaStream_t st) {
-  auto kern = k_fused_query<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX>;
-  const size_t smem = smem_bytes_for<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX>(a.w_bytes);
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "fused query smem %zu: %s", smem, cudaGetErrorString(e));
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
+static nmg_status launch_query_nwg(const FusedArgs& a, cudaStream_t st) {
+  auto kern = k_fused_query<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG>;
+  const size_t smem = smem_bytes_for<F, LEVELS, MODE, SHDEG, BINS, NWG>(a.w_bytes);
+  nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
+  if (s != NMG_OK) return s;
+  const int sms = sm_count();
   const int tiles = (a.n_max + kRows - 1) / kRows;
-  int grid = (tiles + kWG - 1) / kWG;
+  int grid = (tiles + NWG - 1) / NWG;
   if (grid > sms) grid = sms;
   if (grid < 1) grid = 1;
-  kern<<<grid, kWG * kRows, smem, st>>>(a);
+  kern<<<grid, NWG * kRows, smem, st>>>(a);
   return check_launch("k_fused_query");
 }
 
+// Warpgroups per CTA: 4 always fits (registers capped at 128 per thread);
+// 5 and 6 trade registers for more resident warps (K = 8 only: TMEM holds
+// 512 columns).
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
+static nmg_status launch_query(const FusedArgs& a, int nwg, cudaStream_t st) {
+  if constexpr (NOUTMAX <= 64) {
+    if (nwg == 5) return launch_query_nwg<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, 5>(a, st);
+    if (nwg == 6) return launch_query_nwg<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, 6>(a, st);
+  }
+  return launch_query_nwg<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, 4>(a, st);
+}
+
 static nmg_status dispatch_query(nmg_ctx* c, const FusedArgs& a, cudaStream_t st) {
+  const int nwg = c->query_wg > 0 ? c->query_wg : 4;
   switch (fstate(c)->preset) {
-    case 1: return launch_query<2, 16, 1, 4, 4, 8, 48>(a, st);
-    case 2: return launch_query<2, 16, 1, 4, 4, 16, 80>(a, st);
-    case 3: return launch_query<4, 8, 0, 2, 4, 8, 48>(a, st);
+    case 1: return launch_query<2, 16, 1, 4, 4, 8, 48, false>(a, nwg, st);
+    case 2: return launch_query<2, 16, 1, 4, 4, 16, 80, false>(a, nwg, st);
+    case 3: return launch_query<4, 8, 0, 2, 4, 8, 48, true>(a, nwg, st);
   }
   return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
 }
@@ -351,6 +368,100 @@ nmg_status fused_check_errors(nmg_ctx* c) {
     return set_error(NMG_ERR_TIMEOUT, "a fused kernel gave up waiting (code %d)", e);
   }
   return NMG_OK;
+}
+
+
+// ---------------------------------------------------------------- autotuner
+// Candidate CTA shapes of the fused query kernel: 4, 5 or 6 warpgroups
+// (128-query tiles) per CTA, one CTA per SM. More warpgroups hide more
+// gather and MMA latency but cap registers (128, 102, 85 per thread).
+static const int kTileCandidates[3] = {4, 5, 6};
+
+static std::string tune_cache_path() {
+  const char* p = getenv("NMG_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* h = getenv("HOME");
+  return std::string(h && *h ? h : "/tmp") + "/.cache/nmg_tune.txt";
+}
+
+static std::string tune_key(nmg_ctx* c, int n) {
+  cudaDeviceProp prop;
+  cudaGetDeviceProperties(&prop, c->device);
+  int bucket = 0;
+  while ((1 << (bucket + 1)) <= n) ++bucket;  // log2 size class
+  char buf[256];
+  snprintf(buf, sizeof(buf), "%s|sm%d%d|preset%d|fp16=%d|n2^%d", prop.name, prop.major, prop.minor, fstate(c)->preset,
+           c->cfg.path == NMG_PATH_FP16, bucket);
+  for (char* q = buf; *q; ++q)
+    if (*q == ' ') *q = '_';
+  return buf;
+}
+
+static int tune_cache_lookup(const std::string& key) {
+  FILE* f = fopen(tune_cache_path().c_str(), "r");
+  if (!f) return 0;
+  char k[256];
+  int v = 0, found = 0;
+  while (fscanf(f, "%255s %d", k, &v) == 2)
+    if (key == k) found = v;
+  fclose(f);
+  return found;
+}
+
+static void tune_cache_store(const std::string& key, int v) {
+  std::string path = tune_cache_path();
+  std::string dir = path.substr(0, path.find_last_of('/'));
+  if (!dir.empty()) mkdir(dir.c_str(), 0755);
+  FILE* f = fopen(path.c_str(), "a");
+  if (!f) return;
+  fprintf(f, "%s %d\n", key.c_str(), v);
+  fclose(f);
+}
+
+nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
+                          int use_cache, int* chosen, cudaStream_t st) {
+  if (!fstate(c)) return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
+  const std::string key = tune_key(c, n);
+  if (use_cache) {
+    const int v = tune_cache_lookup(key);
+    if (v > 0) {
+      c->query_wg = v;
+      if (chosen) *chosen = v;
+      return NMG_OK;
+    }
+  }
+  cudaEvent_t e0, e1;
+  NMG_CUDA_TRY(cudaEventCreate(&e0));
+  NMG_CUDA_TRY(cudaEventCreate(&e1));
+  float best_ms = 1e30f;
+  int best = 4;
+  const int ncand = fstate(c)->preset == 2 ? 1 : 3;  // K = 16 needs 128 TMEM columns per warpgroup
+  for (int i = 0; i < ncand; ++i) {
+    c->query_wg = kTileCandidates[i];
+    nmg_status s = fused_query(c, in, u4, nullptr, n, out, st);  // warm-up (and shared-memory setup)
+    if (s != NMG_OK) break;
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < 3; ++r) fused_query(c, in, u4, nullptr, n, out, st);
+    cudaEventRecord(e1, st);
+    cudaError_t e = cudaEventSynchronize(e1);
+    if (e != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return set_error(NMG_ERR_CUDA, "autotune: %s", cudaGetErrorString(e));
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = kTileCandidates[i];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->query_wg = best;
+  if (chosen) *chosen = best;
+  if (use_cache) tune_cache_store(key, best);
+  return fused_check_errors(c);
 }
 
 }  // namespace nmg

@@ -7,7 +7,6 @@
 
 namespace nmg {
 
-constexpr int kWG = 4;          // warpgroups per CTA
 constexpr int kRows = 128;      // rows per tile (MMA M)
 
 struct FusedArgs {
@@ -107,9 +106,67 @@ NMG_D void load_feats(const uint16_t* table, uint32_t entry, float* v, bool fp16
   }
 }
 
+// Features of grid level l at position p3 (F values into out). The cell and
+// weights follow grid.h:221-385; the corner indices are formed from per-axis
+// terms (x, y*P1, z*P2 for hashed levels, x, y*res, z*res^2 for dense ones),
+// which equal grid_index's value for every corner, and the corner weight is
+// (w_x' * w_y') * w_z' as in the reference.
+template <int F, bool SMOOTH>
+NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* out) {
+  float w[3];
+  uint32_t g[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const float pp = __fadd_rn(__fmul_rn(p3[d], a.enc.scale[l]), 0.5f);
+    const float fl = floorf(pp);
+    g[d] = uint32_t(int(fl));
+    const float f = pp - fl;
+    w[d] = SMOOTH ? f * f * (3.f - 2.f * f) : f;
+  }
+  const float wxy[4] = {(1.f - w[0]) * (1.f - w[1]), w[0] * (1.f - w[1]), (1.f - w[0]) * w[1], w[0] * w[1]};
+  const float wz[2] = {1.f - w[2], w[2]};
+  const uint32_t T = a.lvl_T[l];
+  const uint32_t base = a.enc.offset[l];
+  uint32_t e[8];
+  if ((a.lvl_hash >> l) & 1u) {
+    const uint32_t mask = T - 1u;
+    const uint32_t hy0 = g[1] * 2654435761u, hz0 = g[2] * 805459861u;
+    const uint32_t hx[2] = {g[0], g[0] + 1u};
+    const uint32_t hy[2] = {hy0, hy0 + 2654435761u};
+    const uint32_t hz[2] = {hz0, hz0 + 805459861u};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) e[c] = base + ((hx[c & 1] ^ hy[(c >> 1) & 1] ^ hz[c >> 2]) & mask);
+  } else {
+    const uint32_t res = a.enc.res[l], r2 = res * res;
+    const uint32_t dy0 = g[1] * res, dz0 = g[2] * r2;
+    const uint32_t dx[2] = {g[0], g[0] + 1u};
+    const uint32_t dy[2] = {dy0, dy0 + res};
+    const uint32_t dz[2] = {dz0, dz0 + r2};
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      uint32_t idx = dx[c & 1] + dy[(c >> 1) & 1] + dz[c >> 2];
+      if (idx >= T) idx %= T;
+      e[c] = base + idx;
+    }
+  }
+  float acc[F];
+#pragma unroll
+  for (int k = 0; k < F; ++k) acc[k] = 0.f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const float wt = wxy[c & 3] * wz[c >> 2];
+    float v[F];
+    load_feats<F>(a.table, e[c], v, a.fp16 != 0);
+#pragma unroll
+    for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < F; ++k) out[k] = acc[k];
+}
+
 // Encodes one input row x into `tile` row `row` (KC 16-byte chunks).
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS>
-NMG_D void encode_row(const FusedArgs& a, const float* x, uint8_t* tile, int row) {
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH>
+NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, int row) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NGRID = LEVELS * F;
   constexpr int NPAD = (NGRID + NDIR + 15) / 16 * 16;
@@ -122,28 +179,7 @@ NMG_D void encode_row(const FusedArgs& a, const float* x, uint8_t* tile, int row
   for (int ch = 0; ch < NGRID / 8; ++ch) {
     float f[8];
 #pragma unroll
-    for (int j = 0; j < LPC; ++j) {
-      const int l = ch * LPC + j;
-      float w[3];
-      uint32_t g[3];
-#pragma unroll
-      for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[l], a.enc.smoothstep, &w[d], &g[d]);
-      float acc[F];
-#pragma unroll
-      for (int k = 0; k < F; ++k) acc[k] = 0.f;
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const float wt = ((c & 1) ? w[0] : 1.f - w[0]) * ((c & 2) ? w[1] : 1.f - w[1]) * ((c & 4) ? w[2] : 1.f - w[2]);
-        const uint32_t e = a.enc.offset[l] +
-                           level_index(a, l, g[0] + (c & 1), g[1] + ((c >> 1) & 1), g[2] + ((c >> 2) & 1));
-        float v[F];
-        load_feats<F>(a.table, e, v, fp16);
-#pragma unroll
-        for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
-      }
-#pragma unroll
-      for (int k = 0; k < F; ++k) f[j * F + k] = acc[k];
-    }
+    for (int j = 0; j < LPC; ++j) grid_level<F, SMOOTH>(a, ch * LPC + j, p3, f + j * F);
     store_chunk(tile, row, ch, KC, f, fp16);
   }
   float d[NPAD - NGRID];
@@ -159,6 +195,12 @@ NMG_D void encode_row(const FusedArgs& a, const float* x, uint8_t* tile, int row
   for (int k = NDIR; k < NPAD - NGRID; ++k) d[k] = 1.f;
 #pragma unroll
   for (int ch = 0; ch < (NPAD - NGRID) / 8; ++ch) store_chunk(tile, row, NGRID / 8 + ch, KC, d + 8 * ch, fp16);
+}
+
+// Loads network input row q (n_input <= 10 floats) with compile-time indices.
+NMG_D void load_row(const float* x, long q, int n_input, float (&v)[10]) {
+#pragma unroll
+  for (int d = 0; d < 10; ++d) v[d] = d < n_input ? x[q * n_input + d] : 0.f;
 }
 
 NMG_D f3 face_fwd(f3 n, f3 v) { return dot3(n, v) > 0.f ? n : f3{-n.x, -n.y, -n.z}; }

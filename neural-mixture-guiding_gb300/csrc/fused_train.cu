@@ -91,7 +91,7 @@ NMG_D void load_chunk(const uint8_t* tile, int row, int chunk, int chunks, float
   f[7] = p.y;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
 __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant__ TrainArgs ta) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
@@ -154,9 +154,8 @@ __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant_
     float x[10];
 #pragma unroll
     for (int d = 0; d < 10; ++d) x[d] = 0.f;
-    if (valid)
-      for (int d = 0; d < a.enc.n_input; ++d) x[d] = ta.x[q * a.enc.n_input + d];
-    encode_row<F, LEVELS, MODE, SHDEG, BINS>(a, x, A0, t);
+    if (valid) load_row(ta.x, q, a.enc.n_input, x);
+    encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH>(a, x, A0, t);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     ok = bar_red_and(1, kRows, ok);
@@ -364,16 +363,16 @@ __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant_
   }
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
 static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
-  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX>;
+  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH>;
   constexpr int DW = NOUTMAX > kWidth ? NOUTMAX : kWidth;
   const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) + size_t(kRows) * NENC * 2 +
                       3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2 + 128;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "fused train smem %zu: %s", smem, cudaGetErrorString(e));
+  nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
+  if (s != NMG_OK) return s;
   kern<<<grid, kRows, smem, st>>>(a);
   return check_launch("k_fused_train");
 }
@@ -396,8 +395,7 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   a.n_mlp = c->lay.n_mlp;
   for (int l = 0; l < c->lay.n_layers; ++l) a.layer_elem_off[l] = c->lay.off[l];
   a.partials = c->ws.partials;
-  int sms = 152;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device);
+  const int sms = sm_count();
   const int tiles = (n_max + kRows - 1) / kRows;
   int grid = tiles < sms ? tiles : sms;
   if (grid < 1) grid = 1;
@@ -406,9 +404,9 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   NMG_CUDA_TRY(cudaMemsetAsync(c->ws.partials, 0, sizeof(double) * (c->ws.n_partials / 2), st));
   nmg_status r;
   switch (s->preset) {
-    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48>(a, grid, st); break;
-    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80>(a, grid, st); break;
-    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48>(a, grid, st); break;
+    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false>(a, grid, st); break;
+    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false>(a, grid, st); break;
+    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true>(a, grid, st); break;
     default: return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
   }
   if (r != NMG_OK) return r;

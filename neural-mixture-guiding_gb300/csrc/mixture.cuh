@@ -25,6 +25,22 @@ template <bool FAST> NMG_D void xsincos(float x, float* s, float* c) {
 }
 template <bool FAST> NMG_D float xdiv(float a, float b) { return FAST ? __fdividef(a, b) : a / b; }
 
+// -expm1(-x) = 1 - e^{-x} for x >= 0 without cancellation: a degree-7 Taylor
+// polynomial below x = 0.5 (relative error < 3e-8), 1 - e^{-x} above.
+template <bool FAST> NMG_D float one_minus_exp_neg(float x) {
+  if (!FAST) return -expm1f(-x);
+  if (x >= 0.5f) return 1.f - __expf(-x);
+  return x * (1.f - x * (1.f / 2.f) * (1.f - x * (1.f / 3.f) * (1.f - x * (1.f / 4.f) *
+             (1.f - x * (1.f / 5.f) * (1.f - x * (1.f / 6.f) * (1.f - x * (1.f / 7.f)))))));
+}
+template <bool FAST> NMG_D f3 unit3(f3 a) {
+  if (!FAST) return normalize3(a);
+  const float n2 = dot3(a, a);
+  if (!(n2 > 0.f)) return a;
+  const float r = rsqrtf(n2);
+  return f3{a.x * r, a.y * r, a.z * r};
+}
+
 // train.h:391-415 activations.
 NMG_D float act_exp_clamp(float x) { return fminf(fmaxf(x, -10.f), 15.f); }
 template <bool FAST> NMG_D float logistic(float x) { return xdiv<FAST>(1.f, 1.f + xexp<FAST>(-x)); }
@@ -45,6 +61,7 @@ template <int K> struct Mix {
   float kap[K];   // concentration
   f3 mu[K];       // unit mean direction
   float w[K];     // normalised weight lambda/total
+  float nrm[K];   // vMF normaliser of each lobe (1/4pi for kappa < M_EPSILON)
   float total;
 };
 
@@ -53,7 +70,7 @@ template <int K> struct Mix {
 // The denominator uses -expm1(-2k) below k = 0.5, where 1 - e^{-2k} cancels.
 template <bool FAST> NMG_D float vmf_norm(float k) {
   if (k < NMG_EPS) return NMG_INV_4PI;
-  const float den = k < 0.5f ? -expm1f(-2.f * k) : 1.f - xexp<FAST>(-2.f * k);
+  const float den = FAST ? one_minus_exp_neg<true>(2.f * k) : (k < 0.5f ? -expm1f(-2.f * k) : 1.f - expf(-2.f * k));
   return xdiv<FAST>(k, NMG_TWO_PI * den);
 }
 
@@ -76,7 +93,10 @@ NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
     m.total += m.lam[i];
   }
 #pragma unroll
-  for (int i = 0; i < K; ++i) m.w[i] = m.lam[i] / m.total;
+  for (int i = 0; i < K; ++i) {
+    m.w[i] = m.lam[i] / m.total;
+    m.nrm[i] = vmf_norm<FAST>(m.kap[i]);
+  }
 }
 
 // Same activation from raw outputs held in registers (compile-time indices).
@@ -98,7 +118,10 @@ NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplu
   }
   const float inv = 1.f / m.total;
 #pragma unroll
-  for (int i = 0; i < K; ++i) m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / m.total;
+  for (int i = 0; i < K; ++i) {
+    m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / m.total;
+    m.nrm[i] = vmf_norm<FAST>(m.kap[i]);
+  }
 }
 
 // distribution.h:39-64 + 184-195: product of every lobe with the cosine lobe
@@ -107,34 +130,51 @@ NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplu
 template <int K, bool FAST>
 NMG_D void mix_apply_cosine(Mix<K>& m, f3 n) {
   const float kb = 2.18853f;
-  f3 mb = normalize3(n);
+  const f3 mb = unit3<FAST>(n);
+  // product normaliser (distribution.h:40-42): 1/4pi below kappa = 1e-3
   auto pnorm = [](float k) {
-    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, -expm1f(-2.f * k));
+    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, one_minus_exp_neg<FAST>(2.f * k));
   };
   const float nb = pnorm(kb);
   m.total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    f3 ma = m.mu[i];
-    float ka = m.kap[i];
+    const f3 ma = m.mu[i];
+    const float ka = m.kap[i];
     f3 nm = add3(scale3(ma, ka), scale3(mb, kb));
-    float nk = sqrtf(dot3(nm, nm));
-    if (nk >= 1e-3f) {
-      nm = f3{nm.x / nk, nm.y / nk, nm.z / nk};
+    const float n2 = dot3(nm, nm);
+    float nk;
+    if (FAST) {
+      const float rn = rsqrtf(n2);
+      nk = n2 * rn;
+      if (nk >= 1e-3f) {
+        nm = scale3(nm, rn);
+      } else {
+        nk = 0.f;
+        nm = ma;
+      }
     } else {
-      nk = 0.f;
-      nm = ma;
+      nk = sqrtf(n2);
+      if (nk >= 1e-3f) {
+        nm = f3{nm.x / nk, nm.y / nk, nm.z / nk};
+      } else {
+        nk = 0.f;
+        nm = ma;
+      }
     }
-    float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
-    float s = xdiv<FAST>(pnorm(ka) * nb, pnorm(nk)) * e;
+    const float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
+    const float pk = pnorm(nk);
+    const float s = xdiv<FAST>(pnorm(ka) * nb, pk) * e;
     m.lam[i] = s * m.lam[i];
     m.kap[i] = nk;
     m.mu[i] = nm;
+    m.nrm[i] = pk;  // equals vmf_norm(nk): nk is 0 or >= 1e-3 here
     m.total += m.lam[i];
   }
   m.total = fmaxf(m.total, NMG_EPS);
+  const float inv = 1.f / m.total;
 #pragma unroll
-  for (int i = 0; i < K; ++i) m.w[i] = m.lam[i] / m.total;
+  for (int i = 0; i < K; ++i) m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / m.total;
 }
 
 // distribution.h:132-140: lobe selection by sequential CDF subtraction,
@@ -198,8 +238,8 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
   unsigned xm = ((ax - ay) < 0.f) & ((ax - az) < 0.f);
   unsigned ym = (1u ^ xm) & ((ay - az) < 0.f);
   unsigned zm = 1u ^ (xm | ym);
-  f3 t = normalize3(cross3(mu, f3{float(xm), float(ym), float(zm)}));
-  f3 b = normalize3(cross3(mu, t));
+  f3 t = unit3<FAST>(cross3(mu, f3{float(xm), float(ym), float(zm)}));
+  f3 b = unit3<FAST>(cross3(mu, t));
   return f3{t.x * loc.x + b.x * loc.y + mu.x * loc.z, t.y * loc.x + b.y * loc.y + mu.y * loc.z,
             t.z * loc.x + b.z * loc.y + mu.z * loc.z};
 }
@@ -210,9 +250,9 @@ NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
   float p = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    float k = m.kap[i];
-    float c = dot3(wi, m.mu[i]);
-    float v = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, c - 1.f)) * vmf_norm<FAST>(k);
+    const float k = m.kap[i];
+    const float c = dot3(wi, m.mu[i]);
+    const float v = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, c - 1.f)) * m.nrm[i];
     p += m.w[i] * v;
   }
   return p;

@@ -436,6 +436,30 @@ nmg_status nmg_network_vjp(nmg_ctx* c, const float* x, const float* draw, int n,
   return plain_vjp(c, x, draw, n, raw, dparams, (cudaStream_t)stream);
 }
 
+nmg_status nmg_set_query_tiling(nmg_ctx* c, int warpgroups_per_cta) {
+  NMG_REQUIRE(c != nullptr, "ctx is NULL");
+  NMG_REQUIRE(warpgroups_per_cta == 0 || (warpgroups_per_cta >= 4 && warpgroups_per_cta <= 6),
+              "warpgroups_per_cta=%d (0 = default, 4..6)", warpgroups_per_cta);
+  NMG_REQUIRE(warpgroups_per_cta <= 4 || c->lay.n_out_pad <= 64, "more than 4 warpgroups needs <= 64 outputs");
+  c->query_wg = warpgroups_per_cta;
+  return NMG_OK;
+}
+
+int nmg_get_query_tiling(const nmg_ctx* c) { return c ? (c->query_wg > 0 ? c->query_wg : 4) : -1; }
+
+nmg_status nmg_autotune_query(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
+                              int use_cache, int* chosen, nmg_stream stream) {
+  NMG_REQUIRE(c && in && out && u4, "NULL argument");
+  nmg_status s = need(c, n, false);
+  if (s != NMG_OK) return s;
+  NMG_REQUIRE(n > 0, "n must be positive");
+  if (c->cfg.path == NMG_PATH_FP32) {
+    if (chosen) *chosen = 0;
+    return NMG_OK;  // the plain path has no tunable tiling
+  }
+  return fused_autotune(c, in, u4, n, out, use_cache, chosen, (cudaStream_t)stream);
+}
+
 nmg_status nmg_check_errors(nmg_ctx* c) {
   NMG_REQUIRE(c != nullptr, "ctx is NULL");
   NMG_CUDA_TRY(cudaDeviceSynchronize());

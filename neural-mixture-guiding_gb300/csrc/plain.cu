@@ -374,7 +374,8 @@ static nmg_status launch_linear(int mode, int epi, const float* X, int ldx, int 
 #define L(M, E)                                                                                           \
   do {                                                                                                    \
     auto kern = k_linear<M, E>;                                                                           \
-    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));                  \
+    nmg_status s_ = ensure_smem(reinterpret_cast<const void*>(kern), smem);                              \
+    if (s_ != NMG_OK) return s_;                                                                          \
     kern<<<blocks, threads, smem, st>>>(X, ldx, nin, W, nout, Y, ldy, H, ldh, d_count, n_max);            \
   } while (0)
   if (mode == 0 && epi == 0) L(0, 0);

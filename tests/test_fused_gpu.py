@@ -219,3 +219,29 @@ def test_fused_train_large_batch_and_ragged(field, synth):
     assert np.all(np.isfinite(s1)) and np.all(np.isfinite(s2))
     f.L.nmg_check_errors.argtypes = [__import__("ctypes").c_void_p]
     assert f.L.nmg_check_errors(f.h) == 0
+
+
+def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
+    """Every CTA tiling of the fused query kernel computes the same outputs; the autotuner picks one
+    of them and caches it."""
+    import torch
+    monkeypatch.setenv("NMG_TUNE_CACHE", str(tmp_path / "tune.txt"))
+    f = nmg.GuidingField(nmg.config(1, path=1), max_queries=50000)
+    q = synth.wavefront(50000, seed=21)
+    pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
+    ref = None
+    for wg in (4, 5, 6):
+        f.set_query_tiling(wg)
+        out = f.query(pos, wo, n, r, u4, want_raw=True)
+        if ref is None:
+            ref = out
+        else:
+            for k in ("dir", "pdf", "lobe", "raw", "selection"):
+                assert torch.equal(out[k], ref[k]), (wg, k)
+    chosen = f.autotune(pos, wo, n, r, u4, use_cache=True)
+    assert chosen in (4, 5, 6) and f.query_tiling == chosen
+    assert (tmp_path / "tune.txt").read_text().strip().endswith(str(chosen))
+    f.set_query_tiling(0)
+    assert f.autotune(pos, wo, n, r, u4, use_cache=True) == chosen  # served from the cache
+    f.check_errors()
+    f.close()
