@@ -282,47 +282,85 @@ __global__ void k_grid_backward(EncodingParams e, const float* __restrict__ x, c
 // ---------------------------------------------------------------- optimiser
 __global__ void k_step_inc(uint32_t* step) { *step += 1; }
 
-// adam.h:47-119 + ema.h:62-75/102-145 in one pass; also writes the
-// reduced-precision copies of the training and inference weights and FP64
-// partial sums of the squared unscaled gradient.
+// adam.h:47-119 + ema.h:62-75/102-145 in one pass over four parameters per
+// thread (128-bit loads and stores); also writes the reduced-precision copies
+// of the training and inference weights and FP64 partial sums of the squared
+// unscaled gradient. Bias corrections beta^t use exp2(t log2 beta) with the
+// logarithms computed once on the host (adam.h:103 evaluates powf per
+// parameter). Requires n_params and n_matrix to be multiples of 4 (layer
+// widths are multiples of 16).
+struct AdamArgs {
+  long n4;               // n_params / 4
+  long n_matrix;         // parameters that get l2 and never skip
+  float loss_scale, lr, beta1, beta2, eps, l2, ema_decay;
+  float log2_beta1, log2_beta2, log2_decay;
+  int use_ema, fp16;
+};
+
+NMG_D uint32_t pack16(float a, float b, int fp16) {
+  if (fp16) return uint32_t(__half_as_ushort(__float2half_rn(a))) | (uint32_t(__half_as_ushort(__float2half_rn(b))) << 16);
+  return uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(a))) |
+         (uint32_t(__bfloat16_as_ushort(__float2bfloat16_rn(b))) << 16);
+}
+
 template <bool HALF16>
-__global__ void k_adam_ema(long n_params, long n_matrix, const float* __restrict__ grad, float loss_scale, float lr,
-                           float beta1, float beta2, float eps, float l2, float ema_decay, int use_ema,
-                           const uint32_t* __restrict__ d_step, float* __restrict__ w, float* __restrict__ m,
-                           float* __restrict__ v, uint32_t* __restrict__ psteps, float* __restrict__ w_inf,
-                           uint16_t* __restrict__ w16, uint16_t* __restrict__ w16_inf, int fp16,
-                           double* __restrict__ partials) {
+__global__ void __launch_bounds__(256) k_adam_ema(AdamArgs a, const float4* __restrict__ grad,
+                                                  const uint32_t* __restrict__ d_step, float4* __restrict__ w,
+                                                  float4* __restrict__ m, float4* __restrict__ v,
+                                                  uint4* __restrict__ psteps, float4* __restrict__ w_inf,
+                                                  uint2* __restrict__ w16, uint2* __restrict__ w16_inf,
+                                                  double* __restrict__ partials) {
   const uint32_t step = *d_step;
-  const float debias_old = 1.f - powf(ema_decay, float(step - 1));
-  const float debias_new = 1.f / (1.f - powf(ema_decay, float(step)));
+  const float debias_old = 1.f - exp2f(float(step - 1) * a.log2_decay);
+  const float debias_new = 1.f / (1.f - exp2f(float(step) * a.log2_decay));
+  const bool separate_inf = w_inf != w;
   double gn = 0.0;
-  for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < n_params; i += long(gridDim.x) * blockDim.x) {
-    float g = grad[i] / loss_scale;
-    gn += double(g) * double(g);
-    float wi = w[i];
-    const bool skip = (i >= n_matrix) && g == 0.f;
-    if (!skip) {
-      if (i < n_matrix) g += l2 * wi;
-      float mm = beta1 * m[i] + (1.f - beta1) * g;
-      float vv = beta2 * v[i] + (1.f - beta2) * (g * g);
-      m[i] = mm;
-      v[i] = vv;
-      uint32_t t = psteps[i] + 1;
-      psteps[i] = t;
-      float lr_t = lr * sqrtf(1.f - powf(beta2, float(t))) / (1.f - powf(beta1, float(t)));
-      wi = wi - lr_t / (sqrtf(vv) + eps) * mm;
-      w[i] = wi;
+  for (long j = long(blockIdx.x) * blockDim.x + threadIdx.x; j < a.n4; j += long(gridDim.x) * blockDim.x) {
+    const bool matrix = 4 * j < a.n_matrix;
+    const float4 g4 = grad[j];
+    float gg[4] = {g4.x / a.loss_scale, g4.y / a.loss_scale, g4.z / a.loss_scale, g4.w / a.loss_scale};
+    float4 w4 = w[j];
+    float ww[4] = {w4.x, w4.y, w4.z, w4.w};
+    bool any = matrix;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      gn += double(gg[k]) * double(gg[k]);
+      any |= gg[k] != 0.f;
     }
-    float wv = wi;
-    if (use_ema) {
-      wv = (w_inf[i] * ema_decay * debias_old + wi * (1.f - ema_decay)) * debias_new;
-      w_inf[i] = wv;
-    } else if (w_inf != w) {
-      w_inf[i] = wi;
+    if (any) {
+      float4 m4 = m[j], v4 = v[j];
+      uint4 t4 = psteps[j];
+      float mm[4] = {m4.x, m4.y, m4.z, m4.w}, vv[4] = {v4.x, v4.y, v4.z, v4.w};
+      uint32_t tt[4] = {t4.x, t4.y, t4.z, t4.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        if (!matrix && gg[k] == 0.f) continue;  // non-matrix parameters without gradient keep their state
+        float g = gg[k];
+        if (matrix) g += a.l2 * ww[k];
+        mm[k] = a.beta1 * mm[k] + (1.f - a.beta1) * g;
+        vv[k] = a.beta2 * vv[k] + (1.f - a.beta2) * (g * g);
+        const uint32_t t = ++tt[k];
+        const float lr_t = a.lr * sqrtf(1.f - exp2f(float(t) * a.log2_beta2)) / (1.f - exp2f(float(t) * a.log2_beta1));
+        ww[k] = ww[k] - lr_t / (sqrtf(vv[k]) + a.eps) * mm[k];
+      }
+      m[j] = make_float4(mm[0], mm[1], mm[2], mm[3]);
+      v[j] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+      psteps[j] = make_uint4(tt[0], tt[1], tt[2], tt[3]);
+      w[j] = make_float4(ww[0], ww[1], ww[2], ww[3]);
+    }
+    float wv[4] = {ww[0], ww[1], ww[2], ww[3]};
+    if (a.use_ema) {
+      const float4 e4 = w_inf[j];
+      const float ee[4] = {e4.x, e4.y, e4.z, e4.w};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) wv[k] = (ee[k] * a.ema_decay * debias_old + ww[k] * (1.f - a.ema_decay)) * debias_new;
+      w_inf[j] = make_float4(wv[0], wv[1], wv[2], wv[3]);
+    } else if (separate_inf) {
+      w_inf[j] = make_float4(ww[0], ww[1], ww[2], ww[3]);
     }
     if (HALF16) {
-      w16[i] = fp16 ? __half_as_ushort(__float2half_rn(wi)) : __bfloat16_as_ushort(__float2bfloat16_rn(wi));
-      w16_inf[i] = fp16 ? __half_as_ushort(__float2half_rn(wv)) : __bfloat16_as_ushort(__float2bfloat16_rn(wv));
+      w16[j] = make_uint2(pack16(ww[0], ww[1], a.fp16), pack16(ww[2], ww[3], a.fp16));
+      w16_inf[j] = make_uint2(pack16(wv[0], wv[1], a.fp16), pack16(wv[2], wv[3], a.fp16));
     }
   }
   double s = block_sum(gn);
@@ -509,14 +547,33 @@ nmg_status optimizer_step(nmg_ctx* c, const int* d_count, int n_max, double* sta
   k_step_inc<<<1, 1, 0, st>>>(c->d_step);
   const int nb = 152 * 8;
   double* gp = c->ws.partials + c->ws.n_partials / 2;
+  if (L.n_params % 4 || L.n_mlp % 4) return set_error(NMG_ERR_UNSUPPORTED, "parameter count not a multiple of 4");
+  AdamArgs aa;
+  aa.n4 = L.n_params / 4;
+  aa.n_matrix = L.n_mlp;
+  aa.loss_scale = g.loss_scale;
+  aa.lr = g.learning_rate;
+  aa.beta1 = g.beta1;
+  aa.beta2 = g.beta2;
+  aa.eps = g.epsilon;
+  aa.l2 = g.l2_reg;
+  aa.ema_decay = g.ema_decay;
+  aa.log2_beta1 = log2f(g.beta1);
+  aa.log2_beta2 = log2f(g.beta2);
+  aa.log2_decay = log2f(g.ema_decay);
+  aa.use_ema = g.use_ema;
+  aa.fp16 = g.path == NMG_PATH_FP16;
   if (c->w16)
-    k_adam_ema<true><<<nb, 256, 0, st>>>(L.n_params, L.n_mlp, c->grad, g.loss_scale, g.learning_rate, g.beta1, g.beta2,
-                                         g.epsilon, g.l2_reg, g.ema_decay, g.use_ema, c->d_step, c->w, c->m, c->v,
-                                         c->psteps, c->w_inf, c->w16, c->w16_inf, g.path == NMG_PATH_FP16, gp);
+    k_adam_ema<true><<<nb, 256, 0, st>>>(aa, reinterpret_cast<const float4*>(c->grad), c->d_step,
+                                         reinterpret_cast<float4*>(c->w), reinterpret_cast<float4*>(c->m),
+                                         reinterpret_cast<float4*>(c->v), reinterpret_cast<uint4*>(c->psteps),
+                                         reinterpret_cast<float4*>(c->w_inf), reinterpret_cast<uint2*>(c->w16),
+                                         reinterpret_cast<uint2*>(c->w16_inf), gp);
   else
-    k_adam_ema<false><<<nb, 256, 0, st>>>(L.n_params, L.n_mlp, c->grad, g.loss_scale, g.learning_rate, g.beta1,
-                                          g.beta2, g.epsilon, g.l2_reg, g.ema_decay, g.use_ema, c->d_step, c->w, c->m,
-                                          c->v, c->psteps, c->w_inf, nullptr, nullptr, 0, gp);
+    k_adam_ema<false><<<nb, 256, 0, st>>>(aa, reinterpret_cast<const float4*>(c->grad), c->d_step,
+                                          reinterpret_cast<float4*>(c->w), reinterpret_cast<float4*>(c->m),
+                                          reinterpret_cast<float4*>(c->v), reinterpret_cast<uint4*>(c->psteps),
+                                          reinterpret_cast<float4*>(c->w_inf), nullptr, nullptr, gp);
   NMG_TRY(check_launch("k_adam_ema"));
   if (stats) {
     k_finish_stats<<<1, 256, 0, st>>>(c->ws.partials, c->ws.n_partials / 2, gp, nb, d_count, n_max, stats);
