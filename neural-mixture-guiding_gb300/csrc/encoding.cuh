@@ -29,6 +29,8 @@ struct EncodingParams {
   uint32_t res[kMaxLevels];
   uint32_t offset[kMaxLevels + 1];  // level start, in table entries
   float aabb[6];
+  float center[3];  // centre of the inflated box
+  float inv_size[3];  // 1 / size of the inflated box
 };
 
 // grid.h:171-187 with the coherent-prime hash (grid.h:132-135).
@@ -48,6 +50,13 @@ NMG_D uint32_t grid_index(int hash, uint32_t T, uint32_t res, uint32_t x, uint32
 
 // common_device.h:484-495 (pos_fract) without FMA contraction so the cell
 // index matches the host computation bit for bit.
+NMG_D f3 unit3f(f3 a) {
+  const float n2 = dot3(a, a);
+  if (!(n2 > 0.f)) return a;
+  const float r = rsqrtf(n2);
+  return f3{a.x * r, a.y * r, a.z * r};
+}
+
 NMG_D void pos_fract(float x, float scale, int smooth, float* w, uint32_t* g) {
   float p = __fadd_rn(__fmul_rn(x, scale), 0.5f);
   float fl = floorf(p);
@@ -152,20 +161,29 @@ NMG_D void encode_directional(const EncodingParams& e, const float* x, float* ou
 // train.cu:174-191 (mode 0) / SH-of-normal variant (mode 1): shading data ->
 // network input row x[n_input]. The box is inflated by 0.5% of its diagonal
 // (train.h:173-177).
+// FAST = true uses the box centre / inverse size precomputed on the host
+// and rsqrt normalisation (the fused path); FAST = false evaluates the
+// reference's expressions literally (the FP32 path).
+template <bool FAST = false>
 NMG_D void featurize(const EncodingParams& e, f3 pos, f3 wo, f3 n, float rough, float* x) {
-  f3 dg{e.aabb[3] - e.aabb[0], e.aabb[4] - e.aabb[1], e.aabb[5] - e.aabb[2]};
-  float infl = sqrtf(dot3(dg, dg)) * 0.005f;
   const float p[3] = {pos.x, pos.y, pos.z};
+  if (FAST) {
 #pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    float lo = e.aabb[d] - infl, hi = e.aabb[d + 3] + infl;
-    x[d] = 0.5f + (p[d] - (lo + hi) / 2.f) / (hi - lo);
+    for (int d = 0; d < 3; ++d) x[d] = 0.5f + (p[d] - e.center[d]) * e.inv_size[d];
+  } else {
+    f3 dg{e.aabb[3] - e.aabb[0], e.aabb[4] - e.aabb[1], e.aabb[5] - e.aabb[2]};
+    float infl = sqrtf(dot3(dg, dg)) * 0.005f;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      float lo = e.aabb[d] - infl, hi = e.aabb[d + 3] + infl;
+      x[d] = 0.5f + (p[d] - (lo + hi) / 2.f) / (hi - lo);
+    }
   }
-  f3 w = normalize3(wo);
+  f3 w = FAST ? unit3f(wo) : normalize3(wo);
   x[3] = (w.x + 1.f) * 0.5f;
   x[4] = (w.y + 1.f) * 0.5f;
   x[5] = (w.z + 1.f) * 0.5f;
-  f3 nn = normalize3(n);
+  f3 nn = FAST ? unit3f(n) : normalize3(n);
   if (e.input_mode == 0) {
     float th = acosf(fminf(1.f, fmaxf(-1.f, nn.z)));
     float ph = atan2f(nn.y, nn.x);

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
       if (a.raw_mode)
         load_row(a.x, q, a.enc.n_input, x);
       else
-        featurize(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
+        featurize<true>(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
     }
     encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH>(a, x, A, t);
     tc::fence_proxy_async();
@@ -130,12 +130,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
         for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(lane_addr + c * 16, v + 16 * c);
         tc::tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < kWidth / 8; ++c) {
-          float f[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) f[i] = fmaxf(v[8 * c + i], 0.f);
-          store_chunk(A, t, c, kWidth / 8, f, fp16);
-        }
+        for (int c = 0; c < kWidth / 8; ++c) store_chunk_relu(A, t, c, kWidth / 8, v + 8 * c, fp16);
         tc::fence_proxy_async();
         tc::fence_before_sync();
         ok = bar_red_and(1 + wg, kRows, done);

@@ -80,6 +80,16 @@ NMG_D void oneblob_fixed(float x, float* o) {
   }
 }
 
+// ReLU of 8 accumulator values packed straight into a 16-byte tile chunk.
+NMG_D void store_chunk_relu(uint8_t* tile, int row, int chunk, int chunks, const float* f, bool fp16) {
+  uint4 v;
+  v.x = tc::pack2_relu(f[0], f[1], fp16);
+  v.y = tc::pack2_relu(f[2], f[3], fp16);
+  v.z = tc::pack2_relu(f[4], f[5], fp16);
+  v.w = tc::pack2_relu(f[6], f[7], fp16);
+  *reinterpret_cast<uint4*>(tile + tc::cm_offset(row, chunk, chunks)) = v;
+}
+
 NMG_D void store_chunk(uint8_t* tile, int row, int chunk, int chunks, const float* f, bool fp16) {
   uint4 v;
   v.x = tc::pack2(f[0], f[1], fp16);
@@ -165,7 +175,9 @@ NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* ou
 }
 
 // Encodes one input row x into `tile` row `row` (KC 16-byte chunks).
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH>
+// UNROLL = false keeps one copy of the chunk body (smaller code for kernels
+// whose instruction footprint matters more than the loop overhead).
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH, bool UNROLL = true>
 NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, int row) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NGRID = LEVELS * F;
@@ -175,7 +187,7 @@ NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, i
   static_assert(NGRID % 8 == 0, "grid features must fill whole chunks");
   const bool fp16 = a.fp16 != 0;
   const float p3[3] = {x[0], x[1], x[2]};
-#pragma unroll
+#pragma unroll(UNROLL ? NGRID / 8 : 1)
   for (int ch = 0; ch < NGRID / 8; ++ch) {
     float f[8];
 #pragma unroll

@@ -1,7 +1,12 @@
 // fused_train.cu -- the fused reduced-precision training step on tcgen05.
 //
-// One persistent CTA per SM, one warpgroup (128 threads) walking tiles of
-// 128 training records. For each tile, entirely on chip:
+// One persistent CTA per SM: two compute warpgroups (128 threads each, one per
+// K = 16 configuration) walking tiles of 128 training records, plus one MMA
+// issuer warp. All tensor-core work of the CTA is issued by one thread of that
+// warp, in each warpgroup's order, so the shared weight-gradient accumulators
+// see their MMAs in sequence; a warpgroup signals "operands ready" on an
+// mbarrier and waits on its "done" mbarrier (tcgen05.commit). For each tile,
+// entirely on chip:
 //   encode the input rows into a BF16/FP16 operand tile (A0)
 //   forward:  h0 = relu(A0 W0^T), h1, h2 (kept in shared memory), raw = h2 W3^T
 //   adjoint:  KL loss and dL/draw per record in registers (train.cu:69-124)
@@ -17,9 +22,11 @@
 // After the last tile each CTA adds its TMEM weight gradients into the
 // global gradient. Adam + EMA then run as one streaming kernel.
 //
-// TMEM (512 columns): [0,128) forward/data-gradient accumulator (M = 128);
-// [128,208) dW0, [208,272) dW1, [272,336) dW2, [336,384) dW3^T (M = 64:
-// rows live in lanes 0-15 of each 32-lane subpartition).
+// TMEM (512 columns): one forward/data-gradient accumulator per warpgroup
+// (M = 128; 64 columns, 128 when the output layer is wider), then the shared
+// weight-gradient accumulators dW0 | dW1 | dW2 | dW3^T (M = 64: rows live in
+// lanes 0-15 of each 32-lane subpartition). The layer-0 data gradient is
+// computed for the grid columns only, the only ones with parameters below.
 //
 // Gradient scale: delta is the reference's loss_scale/n scaled gradient
 // (train.cu:80) multiplied by S (n for BF16, min(n, 256) for FP16) to keep
@@ -91,40 +98,75 @@ NMG_D void load_chunk(const uint8_t* tile, int row, int chunk, int chunks, float
   f[7] = p.y;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
-__global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant__ TrainArgs ta) {
+// Number of tiles warpgroup g of this CTA processes (the same expression in
+// the compute warpgroups and in the MMA issuer).
+NMG_D int wg_tiles(int ntiles, int g, int nwg) {
+  const int first = blockIdx.x * nwg + g, stride = gridDim.x * nwg;
+  return first < ntiles ? (ntiles - 1 - first) / stride + 1 : 0;
+}
+
+// Signals the issuer that this warpgroup's operands for its next MMA batch
+// are in shared memory (and that its last TMEM reads are done): every thread
+// makes its writes visible to the tensor core, the group synchronises (and
+// agrees on `ok`), and one thread arrives on the group's ready barrier.
+NMG_D bool signal_ready(int g, int t, uint64_t* ready, bool ok) {
+  tc::fence_proxy_async();
+  tc::fence_before_sync();
+  ok = bar_red_and(1 + g, kRows, ok);
+  if (ok && t == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(ready)) : "memory");
+  return ok;
+}
+
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
+__global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __grid_constant__ TrainArgs ta) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
+  constexpr int NGRID = LEVELS * F;
+  constexpr int DMAX = NOUTMAX > kWidth ? NOUTMAX : kWidth;
   constexpr uint32_t A_BYTES = kRows * NENC * 2;
   constexpr uint32_t H_BYTES = kRows * kWidth * 2;
-  constexpr uint32_t D_BYTES = kRows * (NOUTMAX > kWidth ? NOUTMAX : kWidth) * 2;  // delta tile (output width)
+  constexpr uint32_t D_BYTES = kRows * DMAX * 2;
+  constexpr uint32_t WG_BYTES = A_BYTES + 3 * H_BYTES + D_BYTES;
   constexpr int NL = 4;  // three hidden layers
-  static_assert(LEVELS * F <= 64, "grid features are read from the first 64 columns");
+  // TMEM: one forward/data-gradient accumulator per warpgroup, then the shared
+  // weight-gradient accumulators (M = 64) dW0 | dW1 | dW2 | dW3^T.
+  constexpr uint32_t DCOLS = NOUTMAX <= 64 ? 64 : 128;
+  constexpr uint32_t CW0 = NWG * DCOLS, CW1 = CW0 + NENC, CW2 = CW1 + kWidth, CW3 = CW2 + kWidth;
+  static_assert(CW3 + NOUTMAX <= kTrainCols, "TMEM holds 512 columns");
+  static_assert(NGRID <= 64 && NGRID % 16 == 0, "grid features are read in 16-column groups");
   extern __shared__ __align__(1024) uint8_t smem[];
   const FusedArgs& a = ta.f;
 
   const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
-  const int t = threadIdx.x, warp = t / 32, lane = t % 32;
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const bool issuer = warp == NWG * 4;
+  const int g = issuer ? 0 : threadIdx.x / kRows;
+  const int t = threadIdx.x % kRows;
   uint8_t* wsm = smem;
-  uint8_t* A0 = smem + w_region;
-  uint8_t* Hs = A0 + A_BYTES;              // three hidden tiles
-  uint8_t* Dt = Hs + 3 * H_BYTES;          // delta tile
-  uint64_t* bars = reinterpret_cast<uint64_t*>(Dt + D_BYTES);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 4);
+  uint8_t* A0 = smem + w_region + g * WG_BYTES;
+  uint8_t* Hs = A0 + A_BYTES;  // three hidden tiles
+  uint8_t* Dt = Hs + 3 * H_BYTES;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * WG_BYTES);  // [0] weights, then ready[], done[]
+  uint64_t* ready = bars + 1;
+  uint64_t* done = bars + 1 + NWG;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + 2 * NWG);
   const bool fp16 = a.fp16 != 0;
   const int nout = a.n_out_pad;
   const int KC3 = nout / 8;
 
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     tc::mbar_init(&bars[0], 1);
-    tc::mbar_init(&bars[1], 1);
+    for (int i = 0; i < NWG; ++i) {
+      tc::mbar_init(&ready[i], 1);
+      tc::mbar_init(&done[i], 1);
+    }
     tc::fence_mbar_init();
   }
-  if (t < 32) tc::tmem_alloc(tslot, kTrainCols);
+  if (issuer) tc::tmem_alloc(tslot, kTrainCols);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (t == 0) {
+  if (threadIdx.x == 0) {
     tc::mbar_arrive_expect_tx(&bars[0], a.w_bytes);
     for (uint32_t off = 0; off < a.w_bytes; off += 16384u) {
       const uint32_t nb = a.w_bytes - off < 16384u ? a.w_bytes - off : 16384u;
@@ -135,10 +177,6 @@ __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant_
   ok = __syncthreads_and(ok) != 0;
 
   const uint32_t tbase = *tslot;
-  const uint32_t tD = tbase + kColD;
-  const uint32_t lane_addr = tbase + (uint32_t(warp * 32) << 16);
-  uint64_t* bar = &bars[1];
-  uint32_t phase = 0;
   const int n = fused_count(a.d_count, a.n_max);
   const int ntiles = (n + kRows - 1) / kRows;
   const float scale = n > 0 ? ta.loss_scale / float(n) : 0.f;          // reference gradient scale
@@ -146,121 +184,149 @@ __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant_
   const float inv_S = 1.f / S;
   const uint32_t w_addr = tc::smem_u32(wsm);
   double loss_acc = 0.0;
-  bool first = true;
+  int cta_tiles = 0;
+  for (int i = 0; i < NWG; ++i) cta_tiles += wg_tiles(ntiles, i, NWG);
 
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long q = long(tile) * kRows + t;
-    const bool valid = q < n;
-    float x[10];
-#pragma unroll
-    for (int d = 0; d < 10; ++d) x[d] = 0.f;
-    if (valid) load_row(ta.x, q, a.enc.n_input, x);
-    encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH>(a, x, A0, t);
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    ok = bar_red_and(1, kRows, ok);
-    if (!ok) break;
-
-    // ------------------------------------------------------------ forward
-    float r[NOUTMAX];
-#pragma unroll
-    for (int i = 0; i < NOUTMAX; ++i) r[i] = 0.f;
-    for (int l = 0; l < NL; ++l) {
-      const bool last = l == NL - 1;
-      const int kin = l == 0 ? NENC : kWidth;
-      if (t == 0) {
-        tc::fence_after_sync();
-        const uint32_t a_addr = tc::smem_u32(l == 0 ? A0 : Hs + (l - 1) * H_BYTES);
-        const uint32_t sbo = uint32_t(kin / 8) * 128u;
-        issue_mma_kmajor(tD, a_addr, kin / 8, w_addr + a.layer_off[l], 128u, sbo, 256u, last ? nout : kWidth,
-                         kin / 16, fp16, false);
-        tc::mma_commit(bar);
+  if (issuer) {
+    // ---------------------------------------------------- MMA issuer (one thread)
+    if (lane == 0 && ok) {
+      int remaining[NWG], step[NWG];
+      uint32_t rph[NWG];
+      bool first[4] = {true, true, true, true};
+      bool any = false;
+      for (int i = 0; i < NWG; ++i) {
+        remaining[i] = 8 * wg_tiles(ntiles, i, NWG);
+        step[i] = 0;
+        rph[i] = 0;
+        any |= remaining[i] > 0;
       }
-      const bool done = tc::mbar_wait(bar, phase);
-      phase ^= 1u;
-      tc::fence_after_sync();
-      if (!last) {
-        float v[kWidth];
-#pragma unroll
-        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(lane_addr + kColD + c * 16, v + 16 * c);
-        tc::tmem_wait_ld();
-        uint8_t* H = Hs + l * H_BYTES;
-#pragma unroll
-        for (int c = 0; c < kWidth / 8; ++c) {
-          float fv[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) fv[i] = fmaxf(v[8 * c + i], 0.f);
-          store_chunk(H, t, c, kWidth / 8, fv, fp16);
+      long long last = clock64();
+      while (any) {
+        any = false;
+        for (int i = 0; i < NWG; ++i) {
+          if (remaining[i] <= 0) continue;
+          any = true;
+          if (!tc::mbar_test(&ready[i], rph[i])) continue;
+          rph[i] ^= 1u;
+          last = clock64();
+          tc::fence_after_sync();
+          uint8_t* gA0 = smem + w_region + i * WG_BYTES;
+          uint8_t* gH = gA0 + A_BYTES;
+          uint8_t* gD = gH + 3 * H_BYTES;
+          const uint32_t tD = tbase + i * DCOLS;
+          const int s = step[i];
+          if (s < NL) {  // forward layer s
+            const int kin = s == 0 ? NENC : kWidth;
+            const uint32_t a_addr = tc::smem_u32(s == 0 ? gA0 : gH + (s - 1) * H_BYTES);
+            issue_mma_kmajor(tD, a_addr, kin / 8, w_addr + a.layer_off[s], 128u, uint32_t(kin / 8) * 128u, 256u,
+                             s == NL - 1 ? nout : kWidth, kin / 16, fp16, false);
+          } else {  // backward layer l: weight gradient then data gradient
+            const int l = NL - 1 - (s - NL);
+            const int dchunks = l == NL - 1 ? KC3 : kWidth / 8;
+            const int dwidth = l == NL - 1 ? nout : kWidth;
+            const int in_w = l == 0 ? NENC : kWidth;
+            const uint8_t* hin = l == 0 ? gA0 : gH + (l - 1) * H_BYTES;
+            if (l == NL - 1)
+              issue_wgrad(tbase + CW3, tc::smem_u32(hin), kWidth / 8, tc::smem_u32(gD), dchunks, dwidth, fp16, !first[l]);
+            else
+              issue_wgrad(tbase + (l == 0 ? CW0 : (l == 1 ? CW1 : CW2)), tc::smem_u32(gD), dchunks, tc::smem_u32(hin),
+                          in_w / 8, in_w, fp16, !first[l]);
+            first[l] = false;
+            // data gradient delta_l W_l (W_l's image as an MN-major operand); for l = 0 only the grid columns
+            const uint32_t wk = uint32_t(in_w / 8) * 128u;
+            issue_mma_kmajor(tD, tc::smem_u32(gD), dchunks, w_addr + a.layer_off[l], wk, 128u, 2u * wk,
+                             l == 0 ? NGRID : in_w, dwidth / 16, fp16, true);
+          }
+          tc::mma_commit(&done[i]);
+          step[i] = (s + 1) % (2 * NL);
+          --remaining[i];
         }
-      } else {
-#pragma unroll
-        for (int c = 0; c < NOUTMAX / 16; ++c)
-          if (c * 16 < nout) tc::tmem_ld16(lane_addr + kColD + c * 16, r + 16 * c);
-        tc::tmem_wait_ld();
+        if (any && clock64() - last > 4000000000LL) {  // no warpgroup signalled for ~2 s
+          atomicExch(a.err, 4);
+          break;
+        }
       }
-      tc::fence_proxy_async();
-      tc::fence_before_sync();
-      ok = bar_red_and(1, kRows, done);
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------- compute warpgroup g
+    uint32_t dph = 0;
+    const uint32_t tD = tbase + g * DCOLS;
+    const uint32_t lane_addr = (uint32_t((warp & 3) * 32) << 16);
+    for (int tile = blockIdx.x * NWG + g; tile < ntiles; tile += gridDim.x * NWG) {
+      const long q = long(tile) * kRows + t;
+      const bool valid = q < n;
+      float x[10];
+#pragma unroll
+      for (int d = 0; d < 10; ++d) x[d] = 0.f;
+      if (valid) load_row(ta.x, q, a.enc.n_input, x);
+      encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, false>(a, x, A0, t);
+      ok = signal_ready(g, t, &ready[g], ok);
       if (!ok) break;
-    }
-    if (!ok) break;
 
-    // ------------------------------------------------- loss and adjoint
-    {
-      float g[NOUTMAX];
+      // ---------------------------------------------------------- forward
+      float r[NOUTMAX];
 #pragma unroll
-      for (int i = 0; i < NOUTMAX; ++i) g[i] = 0.f;
-      if (valid) {
-        float rr[8];
-#pragma unroll
-        for (int j = 0; j < 8; ++j) rr[j] = j < ta.rstride ? ta.rec[q * ta.rstride + j] : 0.f;
-        const float l = tile_loss<K, NOUTMAX>(ta, r, rr, scale, g);
-        loss_acc += double(l);
-      }
-#pragma unroll
-      for (int c = 0; c < NOUTMAX / 8; ++c) {
-        if (c * 8 < nout) {
-          float fv[8];
-#pragma unroll
-          for (int i = 0; i < 8; ++i) fv[i] = g[8 * c + i] * S;
-          store_chunk(Dt, t, c, KC3, fv, fp16);
-        }
-      }
-    }
-    tc::fence_proxy_async();
-    tc::fence_before_sync();
-    ok = bar_red_and(1, kRows, ok);
-    if (!ok) break;
-
-    // ------------------------------------------------------------ backward
-    for (int l = NL - 1; l >= 0; --l) {
-      const int dchunks = l == NL - 1 ? KC3 : kWidth / 8;   // chunks per row of delta_l
-      const int dwidth = l == NL - 1 ? nout : kWidth;       // width of delta_l
-      const int in_w = l == 0 ? NENC : kWidth;               // width of layer l's input
-      const uint8_t* hin = l == 0 ? A0 : Hs + (l - 1) * H_BYTES;
-      if (t == 0) {
+      for (int i = 0; i < NOUTMAX; ++i) r[i] = 0.f;
+      for (int l = 0; l < NL; ++l) {
+        const bool fin = tc::mbar_wait(&done[g], dph);
+        dph ^= 1u;
         tc::fence_after_sync();
-        // weight gradient of layer l
-        if (l == NL - 1) {
-          // dW3^T [in = 64][out] += h2^T delta3
-          issue_wgrad(tbase + kColW3, tc::smem_u32(hin), kWidth / 8, tc::smem_u32(Dt), dchunks, dwidth, fp16, !first);
+        if (l < NL - 1) {
+          float v[kWidth];
+#pragma unroll
+          for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, v + 16 * c);
+          tc::tmem_wait_ld();
+          uint8_t* H = Hs + l * H_BYTES;
+#pragma unroll
+          for (int c = 0; c < kWidth / 8; ++c) store_chunk_relu(H, t, c, kWidth / 8, v + 8 * c, fp16);
+          ok = signal_ready(g, t, &ready[g], fin && ok);
+          if (!ok) break;
         } else {
-          const uint32_t col = l == 0 ? kColW0 : (l == 1 ? kColW1 : kColW2);
-          issue_wgrad(tbase + col, tc::smem_u32(Dt), dchunks, tc::smem_u32(hin), in_w / 8, in_w, fp16, !first);
+#pragma unroll
+          for (int c = 0; c < NOUTMAX / 16; ++c)
+            if (c * 16 < nout) tc::tmem_ld16(tD + lane_addr + c * 16, r + 16 * c);
+          tc::tmem_wait_ld();
+          ok = fin && ok;
         }
-        // data gradient: delta_l [128 x dwidth] times W_l [dwidth x in_w]; W_l's image read as MN-major
-        const uint32_t wk = uint32_t(in_w / 8) * 128u;  // image bytes per 8 rows of W_l (one K group)
-        issue_mma_kmajor(tD, tc::smem_u32(Dt), dchunks, w_addr + a.layer_off[l], wk, 128u, 2u * wk, in_w, dwidth / 16,
-                         fp16, true);
-        tc::mma_commit(bar);
       }
-      const bool done = tc::mbar_wait(bar, phase);
-      phase ^= 1u;
-      tc::fence_after_sync();
-      if (l > 0) {
+      if (!ok) {
+        ok = bar_red_and(1 + g, kRows, false);
+        break;
+      }
+
+      // ------------------------------------------------- loss and adjoint
+      {
+        float gr[NOUTMAX];
+#pragma unroll
+        for (int i = 0; i < NOUTMAX; ++i) gr[i] = 0.f;
+        if (valid) {
+          float rr[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) rr[j] = j < ta.rstride ? ta.rec[q * ta.rstride + j] : 0.f;
+          loss_acc += double(tile_loss<K, NOUTMAX>(ta, r, rr, scale, gr));
+        }
+#pragma unroll
+        for (int c = 0; c < NOUTMAX / 8; ++c) {
+          if (c * 8 < nout) {
+            float fv[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) fv[i] = gr[8 * c + i] * S;
+            store_chunk(Dt, t, c, KC3, fv, fp16);
+          }
+        }
+      }
+      ok = signal_ready(g, t, &ready[g], ok);
+      if (!ok) break;
+
+      // ---------------------------------------------------------- backward
+      for (int l = NL - 1; l >= 1; --l) {
+        const bool fin = tc::mbar_wait(&done[g], dph);
+        dph ^= 1u;
+        tc::fence_after_sync();
         float v[kWidth];
 #pragma unroll
-        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(lane_addr + kColD + c * 16, v + 16 * c);
+        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, v + 16 * c);
         tc::tmem_wait_ld();
         const uint8_t* H = Hs + (l - 1) * H_BYTES;
 #pragma unroll
@@ -271,109 +337,118 @@ __global__ void __launch_bounds__(kRows, 1) k_fused_train(const __grid_constant_
           for (int i = 0; i < 8; ++i) fv[i] = hv[i] > 0.f ? v[8 * c + i] : 0.f;
           store_chunk(Dt, t, c, kWidth / 8, fv, fp16);
         }
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        ok = bar_red_and(1, kRows, done);
+        ok = signal_ready(g, t, &ready[g], fin && ok);
         if (!ok) break;
-      } else {
-        // dL/d(encoded input): the grid columns feed the table gradient
-        float dg[LEVELS * F];
+      }
+      if (!ok) break;
+      // layer 0: dL/d(grid features) -> table gradient
+      {
+        const bool fin = tc::mbar_wait(&done[g], dph);
+        dph ^= 1u;
+        tc::fence_after_sync();
+        float dg[NGRID];
 #pragma unroll
-        for (int c = 0; c < (LEVELS * F + 15) / 16; ++c) tc::tmem_ld16(lane_addr + kColD + c * 16, dg + 16 * c);
+        for (int c = 0; c < NGRID / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, dg + 16 * c);
         tc::tmem_wait_ld();
-        ok = done;
-        if (valid && ok) {
+        ok = bar_red_and(1 + g, kRows, fin && ok);
+        if (!ok) break;
+        // Stage the row's grid gradient in the (now idle) delta tile, column t,
+        // so the level loop below can index it: [feature][row] floats.
+        float* dgs = reinterpret_cast<float*>(Dt);
+        static_assert(NGRID * kRows * 4 <= D_BYTES, "grid gradient staging fits the delta tile");
+#pragma unroll
+        for (int j = 0; j < NGRID; ++j) dgs[j * kRows + t] = dg[j] * inv_S;
+        if (valid) {
           const float p3[3] = {x[0], x[1], x[2]};
           float* gt = ta.grad + ta.n_mlp;
-#pragma unroll
+#pragma unroll 1
           for (int lv = 0; lv < LEVELS; ++lv) {
             float w[3];
             uint32_t gc[3];
 #pragma unroll
-            for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[lv], a.enc.smoothstep, &w[d], &gc[d]);
+            for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[lv], SMOOTH ? 1 : 0, &w[d], &gc[d]);
+            float df[F];
+#pragma unroll
+            for (int k = 0; k < F; ++k) df[k] = dgs[(F * lv + k) * kRows + t];
+            const float wxy[4] = {(1.f - w[0]) * (1.f - w[1]), w[0] * (1.f - w[1]), (1.f - w[0]) * w[1], w[0] * w[1]};
+            const float wz[2] = {1.f - w[2], w[2]};
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
-              const float wt = ((c & 1) ? w[0] : 1.f - w[0]) * ((c & 2) ? w[1] : 1.f - w[1]) *
-                               ((c & 4) ? w[2] : 1.f - w[2]) * inv_S;
+              const float wt = wxy[c & 3] * wz[c >> 2];
               const uint32_t e = a.enc.offset[lv] +
                                  level_index(a, lv, gc[0] + (c & 1), gc[1] + ((c >> 1) & 1), gc[2] + ((c >> 2) & 1));
-              if (F == 2) {
-                atomicAdd(reinterpret_cast<float2*>(gt) + e, make_float2(wt * dg[2 * lv], wt * dg[2 * lv + 1]));
-              } else {
 #pragma unroll
-                for (int k = 0; k < F; k += 2)
-                  atomicAdd(reinterpret_cast<float2*>(gt + size_t(e) * F + k),
-                            make_float2(wt * dg[F * lv + k], wt * dg[F * lv + k + 1]));
-              }
+              for (int k = 0; k < F; k += 2)
+                atomicAdd(reinterpret_cast<float2*>(gt + size_t(e) * F + k), make_float2(wt * df[k], wt * df[k + 1]));
             }
           }
         }
       }
     }
-    if (!ok) break;
-    first = false;
   }
 
-  // ---- flush this CTA's weight gradients (M = 64 accumulators) to global
+  // ---- flush the CTA's weight gradients (M = 64 accumulators) to global
   tc::fence_before_sync();
   ok = __syncthreads_and(ok) != 0;
   tc::fence_after_sync();
-  if (ok && !first) {
-    const int row = warp * 16 + lane;  // valid for lane < 16
-    const uint32_t cols[4] = {kColW0, kColW1, kColW2, kColW3};
-    const int widths[4] = {NENC, kWidth, kWidth, 64};  // dW3^T has out (<= 64 used) columns
-    for (int m = 0; m < 4; ++m) {
+  if (ok && cta_tiles > 0 && !issuer) {
+    const int row = (warp & 3) * 16 + lane;  // valid for lane < 16
+    const uint32_t qaddr = uint32_t((warp & 3) * 32) << 16;
+    const uint32_t cols[4] = {CW0, CW1, CW2, CW3};
+    const int widths[4] = {NENC, kWidth, kWidth, kWidth};
+    for (int m = g; m < 4; m += NWG) {
       const int ncols = m == 3 ? nout : widths[m];
       for (int c0 = 0; c0 < ncols; c0 += 16) {
         float v[16];
-        tc::tmem_ld16(lane_addr + cols[m] + c0, v);
+        tc::tmem_ld16(tbase + qaddr + cols[m] + c0, v);
         tc::tmem_wait_ld();
         if (lane < 16) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int col = c0 + i;
             if (col >= ncols) continue;
-            long idx;
-            if (m < 3)
-              idx = ta.layer_elem_off[m] + long(row) * widths[m] + col;  // dW_m[out = row][in = col]
-            else
-              idx = ta.layer_elem_off[3] + long(col) * kWidth + row;     // W3[out = col][in = row]
+            const long idx = m < 3 ? ta.layer_elem_off[m] + long(row) * widths[m] + col  // dW_m[out = row][in = col]
+                                   : ta.layer_elem_off[3] + long(col) * kWidth + row;   // W3[out = col][in = row]
             atomicAdd(ta.grad + idx, v[i] * inv_S);
           }
         }
       }
     }
   }
-  if (!ok && t == 0) atomicExch(a.err, 3);
+  if (!ok && threadIdx.x == 0) atomicExch(a.err, 3);
   // loss partial sum of this CTA
   {
-    __shared__ double red[4];
-    double v = loss_acc;
+    __shared__ double red[NWG * 4 + 1];
+    double v = issuer ? 0.0 : loss_acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp] = v;
     __syncthreads();
-    if (t == 0) ta.partials[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int i = 0; i < NWG * 4; ++i) s += red[i];
+      ta.partials[blockIdx.x] = s;
+    }
   }
   tc::fence_before_sync();
   __syncthreads();
-  if (t < 32) {
+  if (issuer) {
     tc::fence_after_sync();
     tc::tmem_dealloc(tbase, kTrainCols);
   }
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
 static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
-  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH>;
   constexpr int DW = NOUTMAX > kWidth ? NOUTMAX : kWidth;
-  const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) + size_t(kRows) * NENC * 2 +
-                      3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2 + 128;
+  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG>;
+  const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) +
+                      NWG * (size_t(kRows) * NENC * 2 + 3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2) + 256;
   nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
   if (s != NMG_OK) return s;
-  kern<<<grid, kRows, smem, st>>>(a);
+  kern<<<grid, NWG * kRows + 32, smem, st>>>(a);
   return check_launch("k_fused_train");
 }
 
@@ -397,16 +472,17 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   a.partials = c->ws.partials;
   const int sms = sm_count();
   const int tiles = (n_max + kRows - 1) / kRows;
-  int grid = tiles < sms ? tiles : sms;
+  const int per_cta = s->preset == 2 ? 1 : 2;  // warpgroups (tiles in flight) per CTA
+  int grid = (tiles + per_cta - 1) / per_cta < sms ? (tiles + per_cta - 1) / per_cta : sms;
   if (grid < 1) grid = 1;
   if (grid > c->ws.n_partials / 2) grid = c->ws.n_partials / 2;
   NMG_CUDA_TRY(cudaMemsetAsync(c->grad, 0, sizeof(float) * size_t(c->lay.n_params), st));
   NMG_CUDA_TRY(cudaMemsetAsync(c->ws.partials, 0, sizeof(double) * (c->ws.n_partials / 2), st));
   nmg_status r;
   switch (s->preset) {
-    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false>(a, grid, st); break;
-    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false>(a, grid, st); break;
-    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true>(a, grid, st); break;
+    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false, 2>(a, grid, st); break;
+    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false, 1>(a, grid, st); break;
+    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true, 2>(a, grid, st); break;
     default: return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
   }
   if (r != NMG_OK) return r;

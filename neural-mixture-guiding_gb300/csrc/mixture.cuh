@@ -164,7 +164,9 @@ NMG_D void mix_apply_cosine(Mix<K>& m, f3 n) {
     }
     const float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
     const float pk = pnorm(nk);
-    const float s = xdiv<FAST>(pnorm(ka) * nb, pk) * e;
+    // pnorm(ka) equals the lobe's cached vMF normaliser above kappa = 1e-3
+    const float pa = FAST ? (ka < 1e-3f ? NMG_INV_4PI : m.nrm[i]) : pnorm(ka);
+    const float s = xdiv<FAST>(pa * nb, pk) * e;
     m.lam[i] = s * m.lam[i];
     m.kap[i] = nk;
     m.mu[i] = nm;
@@ -219,7 +221,7 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
   // 1 + cos = log1p((1 - u0) expm1(2k)) / k, so that sin^2 = (1-cos)(1+cos)
   // keeps its digits near both poles of the lobe (k < 8.3 there, so
   // expm1(2k) stays finite).
-  const float omc = -log1pf(u0 * expm1f(-2.f * k)) / k;
+  const float omc = -log1pf(-u0 * one_minus_exp_neg<FAST>(2.f * k)) / k;
   float ct, s2;
   if (omc <= 1.f) {
     ct = 1.f - omc;

@@ -75,6 +75,15 @@ static nmg_status derive(const nmg_config& c, EncodingParams& e, Layout& L) {
   NMG_REQUIRE(e.n_enc_pad <= 128, "encoded width %d above 128", e.n_enc_pad);
   NMG_REQUIRE(e.n_enc_pad - grid <= 64, "non-grid encoded width above 64");
   for (int i = 0; i < 6; ++i) e.aabb[i] = c.aabb[i];
+  {  // inflated box (train.h:173-177), same float expressions as the device code
+    const float dx = c.aabb[3] - c.aabb[0], dy = c.aabb[4] - c.aabb[1], dz = c.aabb[5] - c.aabb[2];
+    const float infl = sqrtf(dx * dx + (dy * dy + dz * dz)) * 0.005f;
+    for (int d = 0; d < 3; ++d) {
+      const float lo = c.aabb[d] - infl, hi = c.aabb[d + 3] + infl;
+      e.center[d] = (lo + hi) / 2.f;
+      e.inv_size[d] = 1.f / (hi - lo);
+    }
+  }
   long n_entries = 0;
   grid_geometry(c, e, &n_entries);
   memset(&L, 0, sizeof(L));

@@ -32,7 +32,21 @@ NMG_D bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   uint32_t ok;
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
-      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity), "r"(1000000u)  // suspend up to 1 ms per attempt instead of spinning
+      : "memory");
+  return ok != 0;
+}
+
+// Non-blocking test of phase `parity` (for a thread that polls several
+// barriers and must not be suspended on any one of them).
+NMG_D bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
       "selp.u32 %0, 1, 0, p;\n\t}"
       : "=r"(ok)
       : "r"(smem_u32(bar)), "r"(parity)
@@ -140,6 +154,16 @@ NMG_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "m
 
 // Named barrier over `count` threads (a warpgroup = 128).
 NMG_D void bar_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+
+// max(a,0), max(b,0) packed into one bf16x2 / f16x2 word in one instruction.
+NMG_D uint32_t pack2_relu(float a, float b, bool fp16) {
+  uint32_t r;
+  if (fp16)
+    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  else
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  return r;
+}
 
 // Packs two floats into a bf16x2 / f16x2 word (low half = a).
 NMG_D uint32_t pack2(float a, float b, bool fp16) {

@@ -16,6 +16,7 @@ PKG = "neural-mixture-guiding_gb300"
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU; exercises the CUDA path through the C ABI")
+    config.addinivalue_line("markers", "slow: long CPU-side check, run with --runslow")
 
 
 def _has_gpu():
@@ -27,6 +28,7 @@ def _has_gpu():
 
 
 def pytest_collection_modifyitems(config, items):
+    _mark_slow(config, items)
     if _has_gpu():
         return
     skip = pytest.mark.skip(reason="no CUDA device")
@@ -55,3 +57,19 @@ def oracle():
 def golden():
     import numpy as np
     return dict(np.load(os.path.join(ROOT, "tests", "golden", "mixture_golden.npz")))
+
+
+def pytest_addoption(parser):
+    parser.addoption("--runslow", action="store_true", default=False, help="run tests marked slow")
+
+
+def _mark_slow(config, items):
+    if config.getoption("--runslow"):
+        return
+    import os
+    if os.environ.get("NMG_RUN_SLOW") == "1":
+        return
+    skip = pytest.mark.skip(reason="slow CPU test (use --runslow)")
+    for it in items:
+        if "slow" in it.keywords:
+            it.add_marker(skip)
