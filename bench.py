@@ -38,6 +38,9 @@ N_QUERIES = 1920 * 1080
 N_TRAIN = 1 << 18
 FLOP_PER_QUERY = 2 * (80 * 64 + 64 * 64 + 64 * 64 + 64 * 48)  # 32,768 executed (padded) MLP FLOP
 BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, rough, u4 in; dir, pdf, lobe, sel out
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query launch over the same 2,073,600-query
+# wavefront (ncu capture summarised in profiles/k_fused_query_hashgrid_2073600.md)
+TRAFFIC_QUERY_BYTES = 141_467_904 + 37_670_400
 
 
 def peaks():
@@ -96,7 +99,8 @@ class Clocks:
                     reasons.add(nm)
         sm.sort()
         return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "200 ms samples under the same load, from before the timed steps to after them"}
 
 
 def dist_setup():
@@ -153,10 +157,25 @@ def run_ours(args):
             f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
             f.train_step(dx, drec, stats=stats)
         torch.cuda.synchronize()
+
+        def untimed_until(n_samples, limit_s):
+            # keeps the GPU under the same load until the sampler has n_samples clock readings
+            t_end = time.perf_counter() + limit_s
+            while len(clocks.lines) < n_samples and time.perf_counter() < t_end:
+                for _ in range(20):
+                    f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
+                    f.train_step(dx, drec, stats=stats)
+                torch.cuda.synchronize()
+
+        if clocks:
+            # clock samples bracket the timed steps: at least two readings under load before them
+            # and two after (the timed region itself is shorter than the sampling interval)
+            clocks.start()
+            untimed_until(2, 10.0)
+            before = len(clocks.lines)
+        torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
-        if clocks:
-            clocks.start()
         t0 = time.perf_counter()
         for i in range(steps):
             flush.fill_(i & 0xff)
@@ -170,6 +189,8 @@ def run_ours(args):
         wall = time.perf_counter() - t0
         if ws > 1:
             torch.distributed.barrier()
+        if clocks:
+            untimed_until(before + 2, 5.0)
         cl = clocks.stop() if clocks else None
         tq = sum(a.elapsed_time(b) for a, b, _ in ev) / 1e3
         tt = sum(b.elapsed_time(c) for _, b, c in ev) / 1e3
@@ -183,33 +204,35 @@ def run_ours(args):
 
     ours = measure(path, args.steps, args.warmup, Clocks())
     plain = measure(nmg.PATH_FP32, max(1, min(args.steps, 3)), 1) if path != nmg.PATH_FP32 else ours
+    frame = frame_graph(nmg, synth, torch, np, dx, drec, path) if path != nmg.PATH_FP32 and not args.no_frame else None
 
-    # end to end through the public API: pinned host inputs in, host results out, every step
+    # end to end through the public API on host buffers (nmg_query_host / nmg_train_step_host): pinned host
+    # inputs in, host results out, every step; the library pipelines the copies with the kernels
     f = ours["field"]
     hq = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in q.items()}
     hx, hrec = torch.from_numpy(x).pin_memory(), torch.from_numpy(rec).pin_memory()
-    hout_dir = torch.empty((N_QUERIES, 3)).pin_memory()
-    hout_pdf = torch.empty(N_QUERIES).pin_memory()
+    hout = {"dir": torch.empty((N_QUERIES, 3)).pin_memory(), "pdf": torch.empty(N_QUERIES).pin_memory(),
+            "lobe": torch.empty(N_QUERIES, dtype=torch.int32).pin_memory(),
+            "selection": torch.empty(N_QUERIES).pin_memory()}
     hstats = torch.empty(2, dtype=torch.float64).pin_memory()
     h2d = sum(t.numel() * t.element_size() for k, t in hq.items() if k != "aabb") + hx.numel() * 4 + hrec.numel() * 4
-    d2h = hout_dir.numel() * 4 + hout_pdf.numel() * 4 + 16
+    d2h = sum(t.numel() * t.element_size() for t in hout.values()) + hstats.numel() * 8
+
+    def e2e_step():
+        f.query_host(hq["pos"], hq["wo"], hq["normal"], hq["rough"], hq["u4"], hout)
+        f.train_step_host(hx, hrec, stats=hstats)
+
+    e2e_step()  # first call allocates the device staging
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
     e2e_steps = max(1, min(args.steps, 5))
     e0.record()
     for _ in range(e2e_steps):
-        for k in ("pos", "wo", "normal", "rough", "u4"):
-            dq[k].copy_(hq[k], non_blocking=True)
-        dx.copy_(hx, non_blocking=True)
-        drec.copy_(hrec, non_blocking=True)
-        o = f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=ours["out"])
-        s = f.train_step(dx, drec)
-        hout_dir.copy_(o["dir"], non_blocking=True)
-        hout_pdf.copy_(o["pdf"], non_blocking=True)
-        hstats.copy_(s, non_blocking=True)
+        e2e_step()
     e1.record()
     torch.cuda.synchronize()
     t_e2e = barrier_max(e0.elapsed_time(e1) / 1e3, ws)
+    e2e_loss = float(hstats[0])
 
     # kernel-only timing of the fused query kernel (dominant kernel) on its own stream
     st = torch.cuda.current_stream()
@@ -263,19 +286,77 @@ def run_ours(args):
         "speedup_vs_plain_fp32": {"queries": qps / ws / plain_qps, "train": tps / ws / plain_tps},
         "final_stats": {"mean_loss": ours["loss"][0], "grad_norm": ours["loss"][1]},
         "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s (query + train step, host buffers)",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "api": "nmg_query_host + nmg_train_step_host (pinned host memory)", "final_loss": e2e_loss},
         "gpu_launches": None,
         "roofline": {"kernel": "k_fused_query" if path != nmg.PATH_FP32 else "plain query kernels",
                      "bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",
-                     "frac": tflops / bf16, "peak_source": src, "traffic": None,
+                     "frac": tflops / bf16, "peak_source": src,
+                     "traffic": TRAFFIC_QUERY_BYTES if path == nmg.PATH_BF16 else None,
+                     "traffic_unit": "bytes per launch (ncu)",
+                     "limiter": "SM issue and L2 gather latency (16 warps/SM, long_scoreboard), not HBM or tensor",
                      "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm,
                      "per_unit": {"flop_per_query": FLOP_PER_QUERY, "hbm_bytes_per_query": BYTES_PER_QUERY},
                      "kernel_ms": t_kernel * 1e3},
         "cpu_baseline": cpu,
         "clocks": ours["clocks"],
+        "frame_graph": frame,
     }
     line["gpu_launches"] = launches_per_step(path) * steps
     print(json.dumps(line), flush=True)
+
+
+BOUNCE_SIZES = [2_073_600, 1_400_000, 900_000, 550_000, 300_000, 150_000, 70_000]
+
+
+def frame_graph(nmg, synth, torch, np, dx, drec, path, lobes=(8, 16), frames=5, warmup=3):
+    """The uneven 7-bounce frame (queues of 2,073,600 ... 70,000 queries, each followed by a 2^18-record
+    training step) captured once as a CUDA graph and replayed; the same frame issued launch by launch is
+    timed beside it. Inputs of a frame (5.4 M queries, 0.44 GB) exceed L2, so no flush is needed."""
+    qs = []
+    for i, n in enumerate(BOUNCE_SIZES):
+        q = synth.wavefront(n, seed=7272 + 100 + i)
+        qs.append({k: torch.from_numpy(np.ascontiguousarray(q[k])).cuda() for k in ("pos", "wo", "normal", "rough", "u4")})
+    res = {"bounce_queries": BOUNCE_SIZES, "train_batch": int(dx.shape[0]),
+           "l2": "not flushed: a frame's inputs (0.44 GB) exceed L2"}
+    st = torch.cuda.current_stream()
+    for K in lobes:
+        f = nmg.GuidingField(nmg.config(nmg.PRESET_HASHGRID, path=path, n_lobes=K), max_queries=BOUNCE_SIZES[0],
+                             max_batch=int(dx.shape[0]))
+        outs, bounces = [], []
+        for q in qs:
+            n = q["pos"].shape[0]
+            o = {"dir": torch.empty((n, 3), device="cuda"), "pdf": torch.empty(n, device="cuda"),
+                 "lobe": torch.empty(n, device="cuda", dtype=torch.int32), "selection": torch.empty(n, device="cuda")}
+            outs.append(o)
+            bounces.append(nmg.GuidingField.bounce(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"], o,
+                                                   count=torch.tensor([n], device="cuda", dtype=torch.int32),
+                                                   train=(dx, drec, None, None)))
+        tiling = f.autotune(qs[0]["pos"], qs[0]["wo"], qs[0]["normal"], qs[0]["rough"], qs[0]["u4"])
+        fr = f.capture_frame(bounces)
+
+        def timed(run):
+            for _ in range(warmup):
+                run()
+            torch.cuda.synchronize()
+            a, b = torch.cuda.Event(True), torch.cuda.Event(True)
+            a.record(st)
+            for _ in range(frames):
+                run()
+            b.record(st)
+            torch.cuda.synchronize()
+            return a.elapsed_time(b) / 1e3 / frames
+
+        t_graph = timed(fr.launch)
+        t_eager = timed(lambda: f.run_frame_eager(bounces))
+        f.check_errors()
+        res["K%d" % K] = {"ms_per_frame_graph": t_graph * 1e3, "ms_per_frame_eager": t_eager * 1e3,
+                          "queries_per_s": sum(BOUNCE_SIZES) / t_graph,
+                          "train_samples_per_s": len(BOUNCE_SIZES) * int(dx.shape[0]) / t_graph,
+                          "graph_nodes": fr.nodes, "query_tiling_warpgroups": tiling}
+        fr.close()
+        f.close()
+    return res
 
 
 def launches_per_step(path):
@@ -386,6 +467,7 @@ def main():
     ap.add_argument("--path", default="bf16", choices=["bf16", "fp16", "fp32"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-frame", action="store_true", help="skip the 7-bounce CUDA-graph frame measurement")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

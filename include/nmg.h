@@ -234,6 +234,15 @@ nmg_status nmg_get_info(const nmg_ctx* ctx, nmg_info* info);
  * within capacity allocate nothing and may be captured in a CUDA graph. */
 nmg_status nmg_reserve(nmg_ctx* ctx, int max_queries, int max_batch);
 
+/* Device bytes the field holds: parameters, optimiser state, weight copies
+ * and workspaces. The FP32 path stores each layer's activations of a
+ * training batch (about 1.9 KB per record for the hash-grid network); the
+ * BF16/FP16 paths recompute them inside the fused training kernel, so their
+ * footprint does not grow with max_batch. No reference counterpart (tcnn
+ * allocates every layer's forward activations per training call,
+ * src/ext/tcnn/src/fully_fused_mlp.cu:711,839-853). */
+nmg_status nmg_device_bytes(const nmg_ctx* ctx, uint64_t* bytes);
+
 /* Parameters: [MLP weights, row-major [out][in] per layer | grid table]
  * (network.h:85-100, fully_fused_mlp.cu:855-864). which = 0: training
  * (master FP32) weights; 1: inference weights (the EMA when use_ema).
@@ -290,6 +299,29 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
                           double* stats, nmg_stream stream);
 
 /*
+ * nmg_query and nmg_train_step on HOST buffers (pinned memory gives the
+ * overlap; pageable memory works but copies synchronously). nmg_query_host
+ * splits the wavefront into up to 4 chunks of at least 2^19 queries and
+ * pipelines them over three streams: inputs of chunk i+1 go to the device
+ * while chunk i is computed on `stream` and the outputs of chunk i-1 come
+ * back. Every input and output array (all of in, u4, out->dir, out->pdf and,
+ * when non-NULL, out->lobe and out->selection) is host memory; out->raw must
+ * be NULL. nmg_train_step_host copies x and records to the device and runs
+ * the step; stats (may be NULL) is HOST memory receiving the two FP64
+ * statistics. Both are ordered after the work already on `stream`, and
+ * `stream` waits for their last copy; the host buffers must stay valid until
+ * then. The first call allocates device staging of the reserved capacity
+ * (not capturable); later calls allocate nothing.
+ * Replaces: the host side of the reference's inference/training calls, which
+ * copy nothing themselves (integrator.cpp:627-701 operate on device queues);
+ * no reference counterpart as an entry point.
+ */
+nmg_status nmg_query_host(nmg_ctx* ctx, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
+                          nmg_stream stream);
+nmg_status nmg_train_step_host(nmg_ctx* ctx, const float* x, const float* records, int n, double* stats,
+                               nmg_stream stream);
+
+/*
  * Vector-Jacobian product of the network at the training weights:
  * given x[n][n_input] and dL/draw[n][n_output_padded], writes raw[n][..]
  * (may be NULL) and ACCUMULATES dL/dparams (FP32, unscaled) into dparams.
@@ -306,6 +338,42 @@ nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int 
  */
 nmg_status nmg_set_query_tiling(nmg_ctx* ctx, int warpgroups_per_cta);
 int nmg_get_query_tiling(const nmg_ctx* ctx);
+
+/*
+ * One frame's bounce loop as a CUDA graph. Bounce i runs the guided query of
+ * its queue (device SoA `in`, uniforms u4, queue length *d_count read on the
+ * device, at most n_max; d_count NULL = n_max) and then, when train_x is
+ * non-NULL, one training step on its batch (train_count / train_n_max as for
+ * nmg_train_step; stats may be NULL). nmg_frame_capture records the whole
+ * sequence once (the context must be reserved for every n_max and
+ * train_n_max); nmg_frame_launch replays it on `stream` with one call. Queue
+ * lengths and the optimiser step are read on the device, so one capture
+ * serves every frame as long as the buffers stay where they were.
+ * nmg_frame_run_eager issues the same sequence as individual launches.
+ * Replaces: the per-bounce inferenceStep/trainStep calls of
+ * GuidedPathTracer::render (integrator.cpp:431-438, 463, 627-701), which are
+ * host-driven launches in the reference.
+ */
+typedef struct nmg_bounce {
+  nmg_shading in;
+  const float* u4;
+  const int* d_count;
+  int n_max;
+  nmg_query_out out;
+  const float* train_x;
+  const float* train_records;
+  const int* train_count;
+  int train_n_max;
+  double* stats;
+} nmg_bounce;
+
+typedef struct nmg_frame nmg_frame;
+nmg_status nmg_frame_capture(nmg_ctx* ctx, const nmg_bounce* bounces, int n_bounces, nmg_frame** frame);
+nmg_status nmg_frame_launch(nmg_frame* frame, nmg_stream stream);
+/* Graph nodes (kernel launches and memsets) one replay executes. */
+int nmg_frame_nodes(const nmg_frame* frame);
+void nmg_frame_destroy(nmg_frame* frame);
+nmg_status nmg_frame_run_eager(nmg_ctx* ctx, const nmg_bounce* bounces, int n_bounces, nmg_stream stream);
 
 /*
  * Autotuner: times the fused query kernel on the caller's inputs for every

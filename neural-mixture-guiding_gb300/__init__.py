@@ -155,6 +155,12 @@ class QueryOut(C.Structure):
                 ("selection", C.c_void_p)]
 
 
+class Bounce(C.Structure):
+    _fields_ = [("in_", Shading), ("u4", C.c_void_p), ("d_count", C.c_void_p), ("n_max", C.c_int),
+                ("out", QueryOut), ("train_x", C.c_void_p), ("train_records", C.c_void_p),
+                ("train_count", C.c_void_p), ("train_n_max", C.c_int), ("stats", C.c_void_p)]
+
+
 def _bind_field(L):
     P = C.c_void_p
     sig = {
@@ -163,6 +169,7 @@ def _bind_field(L):
         "nmg_create": [C.POINTER(Config), C.POINTER(P)],
         "nmg_get_info": [P, C.POINTER(Info)],
         "nmg_reserve": [P, C.c_int, C.c_int],
+        "nmg_device_bytes": [P, C.POINTER(C.c_uint64)],
         "nmg_set_params": [P, P, P],
         "nmg_get_params": [P, C.c_int, P, P],
         "nmg_get_gradients": [P, P, P],
@@ -171,6 +178,11 @@ def _bind_field(L):
         "nmg_query": [P, C.POINTER(Shading), P, P, C.c_int, C.POINTER(QueryOut), P],
         "nmg_pdf": [P, C.POINTER(Shading), P, P, C.c_int, P, P],
         "nmg_train_step": [P, P, P, P, C.c_int, P, P],
+        "nmg_query_host": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), P],
+        "nmg_train_step_host": [P, P, P, C.c_int, P, P],
+        "nmg_frame_capture": [P, C.POINTER(Bounce), C.c_int, C.POINTER(P)],
+        "nmg_frame_launch": [P, P],
+        "nmg_frame_run_eager": [P, C.POINTER(Bounce), C.c_int, P],
         "nmg_network_vjp": [P, P, P, C.c_int, P, P, P],
         "nmg_set_query_tiling": [P, C.c_int],
         "nmg_autotune_query": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), C.c_int, C.POINTER(C.c_int), P],
@@ -188,6 +200,10 @@ def _bind_field(L):
     L.nmg_get_step.restype = C.c_int
     L.nmg_get_query_tiling.argtypes = [P]
     L.nmg_get_query_tiling.restype = C.c_int
+    L.nmg_frame_nodes.argtypes = [P]
+    L.nmg_frame_nodes.restype = C.c_int
+    L.nmg_frame_destroy.argtypes = [P]
+    L.nmg_frame_destroy.restype = None
 
 
 def config(preset=PRESET_HASHGRID, **overrides):
@@ -241,6 +257,13 @@ class GuidingField:
 
     def reserve(self, max_queries, max_batch):
         check(self.L.nmg_reserve(self.h, int(max_queries), int(max_batch)))
+
+    @property
+    def device_bytes(self):
+        """Device memory the field holds (parameters, optimiser state, workspaces)."""
+        b = C.c_uint64()
+        check(self.L.nmg_device_bytes(self.h, C.byref(b)))
+        return int(b.value)
 
     @property
     def n_params(self):
@@ -321,6 +344,51 @@ class GuidingField:
                                     _stream(stream)))
         return stats
 
+    def query_host(self, pos, wo, normal, rough, u4, outputs, stream=None):
+        """nmg_query on host tensors (pinned for overlap); outputs: dict of host tensors dir, pdf[, lobe,
+        selection]. Asynchronous on `stream`: synchronise before reading the outputs."""
+        o = QueryOut(*(outputs[k].data_ptr() if outputs.get(k) is not None else None
+                       for k in ("dir", "pdf", "lobe", "raw", "selection")))
+        sh = self.shading(pos, wo, normal, rough)
+        check(self.L.nmg_query_host(self.h, C.byref(sh), _ptr(u4), pos.shape[0], C.byref(o), _stream(stream)))
+        return outputs
+
+    def train_step_host(self, x, records, stats=None, stream=None):
+        """nmg_train_step on host tensors; stats (host float64 [2], may be None) receives the statistics."""
+        check(self.L.nmg_train_step_host(self.h, _ptr(x), _ptr(records), x.shape[0], _ptr(stats), _stream(stream)))
+        return stats
+
+    @staticmethod
+    def bounce(pos, wo, normal, rough, u4, outputs, count=None, n_max=None, train=None):
+        """One bounce of a frame: device tensors of the queue (capacity n_max = pos rows), its device
+        count (int32 tensor or None), output tensors, and optionally a training batch
+        train = (x, records, count or None, stats or None)."""
+        b = Bounce()
+        b.in_ = GuidingField.shading(pos, wo, normal, rough)
+        b.u4 = u4.data_ptr()
+        b.d_count = count.data_ptr() if count is not None else None
+        b.n_max = int(n_max if n_max is not None else pos.shape[0])
+        b.out = QueryOut(*(outputs[k].data_ptr() if outputs.get(k) is not None else None
+                           for k in ("dir", "pdf", "lobe", "raw", "selection")))
+        if train is not None:
+            x, rec, cnt, st = train
+            b.train_x, b.train_records = x.data_ptr(), rec.data_ptr()
+            b.train_count = cnt.data_ptr() if cnt is not None else None
+            b.train_n_max = int(x.shape[0])
+            b.stats = st.data_ptr() if st is not None else None
+        return b
+
+    def capture_frame(self, bounces):
+        """CUDA graph of the bounce loop (nmg_frame_capture); returns a Frame."""
+        arr = (Bounce * len(bounces))(*bounces)
+        h = C.c_void_p()
+        check(self.L.nmg_frame_capture(self.h, arr, len(bounces), C.byref(h)))
+        return Frame(self.L, h, arr)
+
+    def run_frame_eager(self, bounces, stream=None):
+        arr = (Bounce * len(bounces))(*bounces)
+        check(self.L.nmg_frame_run_eager(self.h, arr, len(bounces), _stream(stream)))
+
     def vjp(self, x, draw, dparams=None, stream=None):
         import torch
         n = x.shape[0]
@@ -357,6 +425,31 @@ class GuidingField:
 
     def load(self, path):
         check(self.L.nmg_load(self.h, path.encode()))
+
+
+class Frame:
+    """A captured bounce loop (CUDA graph executable)."""
+
+    def __init__(self, L, h, bounces):
+        self.L, self.h, self._bounces = L, h, bounces
+
+    @property
+    def nodes(self):
+        return self.L.nmg_frame_nodes(self.h)
+
+    def launch(self, stream=None):
+        check(self.L.nmg_frame_launch(self.h, _stream(stream)))
+
+    def close(self):
+        if self.h:
+            self.L.nmg_frame_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def oracle_net_spec(cfg):

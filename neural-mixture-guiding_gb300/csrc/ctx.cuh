@@ -37,6 +37,7 @@ struct Workspace {
   void* fused = nullptr;
   void* fused_dev = nullptr;
   size_t fused_bytes = 0;
+  size_t bytes = 0;  // device bytes of the buffers above except the fused allocation
 };
 
 }  // namespace nmg
@@ -60,6 +61,7 @@ struct nmg_ctx {
   uint16_t* w16_inf = nullptr; // inference weights
   int query_wg = 0;            // warpgroups per CTA of the fused query kernel (0: default)
   nmg::Workspace ws;
+  void* host_io = nullptr;     // streams and staging of the host-buffer entry points (host_io.cu)
 };
 
 namespace nmg {
@@ -96,6 +98,9 @@ nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, in
                           int use_cache, int* chosen, cudaStream_t st);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st);
+
+// host_io.cu
+void host_io_release(nmg_ctx* c);
 
 nmg_status set_error(nmg_status st, const char* fmt, ...);
 

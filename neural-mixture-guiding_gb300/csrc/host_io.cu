@@ -1,0 +1,224 @@
+// host_io.cu -- query and training entry points on HOST buffers.
+//
+// A caller whose wavefront lives in host memory (the reference's CPU-side
+// callers, or a renderer that keeps its queues on the host) would otherwise
+// copy all inputs to the device, run the query, and copy the outputs back,
+// one after another. These entry points split the wavefront into chunks and
+// pipeline them on three streams: chunk i+1's inputs go host->device while
+// chunk i is computed and chunk i-1's outputs go device->host. With pinned
+// host buffers the copies overlap the fused kernel almost entirely.
+//
+// Ordering with the caller's stream: everything starts after the work already
+// queued on `stream` and `stream` waits for the last output copy, so the
+// calls behave like one asynchronous operation on `stream`. The device
+// staging buffers are allocated on the first call (sized to the reserved
+// capacity) and reused; that first call is therefore not capturable.
+#include <string.h>
+
+#include <new>
+
+#include "api_common.cuh"
+#include "ctx.cuh"
+
+namespace nmg {
+
+constexpr int kMaxChunks = 4;
+constexpr int kMinChunk = 1 << 19;  // queries; smaller chunks leave the persistent grid underfilled
+
+struct HostIO {
+  cudaStream_t h2d = nullptr, d2h = nullptr;
+  cudaEvent_t start = nullptr, done = nullptr;
+  cudaEvent_t in_ready[kMaxChunks] = {}, out_ready[kMaxChunks] = {};
+  int cap_q = 0, cap_b = 0;
+  // query staging (SoA, device)
+  float *pos = nullptr, *wo = nullptr, *nrm = nullptr, *rough = nullptr, *u4 = nullptr;
+  float *dir = nullptr, *pdf = nullptr, *sel = nullptr;
+  int* lobe = nullptr;
+  // training staging
+  float *x = nullptr, *rec = nullptr;
+  double* stats = nullptr;  // [2] device copy of the step's statistics
+};
+
+static void free_staging_q(HostIO* h) {
+  for (float* p : {h->pos, h->wo, h->nrm, h->rough, h->u4, h->dir, h->pdf, h->sel}) cudaFree(p);
+  cudaFree(h->lobe);
+  h->pos = h->wo = h->nrm = h->rough = h->u4 = h->dir = h->pdf = h->sel = nullptr;
+  h->lobe = nullptr;
+  h->cap_q = 0;
+}
+
+static void free_staging_b(HostIO* h) {
+  cudaFree(h->x);
+  cudaFree(h->rec);
+  cudaFree(h->stats);
+  h->x = h->rec = nullptr;
+  h->stats = nullptr;
+  h->cap_b = 0;
+}
+
+void host_io_release(nmg_ctx* c) {
+  HostIO* h = static_cast<HostIO*>(c->host_io);
+  if (!h) return;
+  free_staging_q(h);
+  free_staging_b(h);
+  if (h->h2d) cudaStreamDestroy(h->h2d);
+  if (h->d2h) cudaStreamDestroy(h->d2h);
+  if (h->start) cudaEventDestroy(h->start);
+  if (h->done) cudaEventDestroy(h->done);
+  for (int i = 0; i < kMaxChunks; ++i) {
+    if (h->in_ready[i]) cudaEventDestroy(h->in_ready[i]);
+    if (h->out_ready[i]) cudaEventDestroy(h->out_ready[i]);
+  }
+  delete h;
+  c->host_io = nullptr;
+}
+
+static nmg_status host_io_get(nmg_ctx* c, HostIO** out) {
+  HostIO* h = static_cast<HostIO*>(c->host_io);
+  if (!h) {
+    h = new (std::nothrow) HostIO();
+    if (!h) return set_error(NMG_ERR_OOM, "host allocation failed");
+    c->host_io = h;
+    const unsigned ef = cudaEventDisableTiming;
+    bool ok = cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h->start, ef) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h->done, ef) == cudaSuccess;
+    for (int i = 0; ok && i < kMaxChunks; ++i)
+      ok = cudaEventCreateWithFlags(&h->in_ready[i], ef) == cudaSuccess &&
+           cudaEventCreateWithFlags(&h->out_ready[i], ef) == cudaSuccess;
+    if (!ok) {
+      host_io_release(c);
+      return set_error(NMG_ERR_CUDA, "creating the copy streams failed");
+    }
+  }
+  *out = h;
+  return NMG_OK;
+}
+
+template <class T>
+static bool alloc_n(T** p, size_t n) {
+  return cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T)) == cudaSuccess;
+}
+
+static nmg_status ensure_staging_q(HostIO* h, int cap) {
+  if (h->cap_q >= cap) return NMG_OK;
+  free_staging_q(h);
+  const size_t n = size_t(cap);
+  const bool ok = alloc_n(&h->pos, 3 * n) && alloc_n(&h->wo, 3 * n) && alloc_n(&h->nrm, 3 * n) &&
+                  alloc_n(&h->rough, n) && alloc_n(&h->u4, 4 * n) && alloc_n(&h->dir, 3 * n) &&
+                  alloc_n(&h->pdf, n) && alloc_n(&h->sel, n) && alloc_n(&h->lobe, n);
+  if (!ok) {
+    free_staging_q(h);
+    return set_error(NMG_ERR_OOM, "query staging for %d queries", cap);
+  }
+  h->cap_q = cap;
+  return NMG_OK;
+}
+
+static nmg_status ensure_staging_b(HostIO* h, int cap, int n_input, int rfloats) {
+  if (h->cap_b >= cap) return NMG_OK;
+  free_staging_b(h);
+  const bool ok = alloc_n(&h->x, size_t(cap) * n_input) && alloc_n(&h->rec, size_t(cap) * rfloats) &&
+                  alloc_n(&h->stats, 2);
+  if (!ok) {
+    free_staging_b(h);
+    return set_error(NMG_ERR_OOM, "training staging for %d records", cap);
+  }
+  h->cap_b = cap;
+  return NMG_OK;
+}
+
+#define NMG_CU(call)                                                                            \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess) return set_error(NMG_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+static nmg_status h2d(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  NMG_CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+  return NMG_OK;
+}
+static nmg_status d2h(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+  NMG_CU(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+  return NMG_OK;
+}
+
+}  // namespace nmg
+
+using namespace nmg;
+
+extern "C" {
+
+nmg_status nmg_query_host(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
+                          nmg_stream stream) {
+  NMG_REQUIRE(c && in && out, "NULL argument");
+  NMG_REQUIRE(n >= 0 && n <= c->ws.cap_q, "n=%d outside 0..%d (call nmg_reserve)", n, c->ws.cap_q);
+  if (n == 0) return NMG_OK;
+  NMG_REQUIRE(in->pos && in->wo && in->normal && in->roughness && u4 && out->dir && out->pdf,
+              "NULL shading array, uniforms or output");
+  NMG_REQUIRE(!out->raw, "raw outputs are not returned by nmg_query_host (use nmg_query)");
+  HostIO* h = nullptr;
+  nmg_status s = host_io_get(c, &h);
+  if (s != NMG_OK) return s;
+  if ((s = ensure_staging_q(h, c->ws.cap_q)) != NMG_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  NMG_CU(cudaEventRecord(h->start, st));
+  NMG_CU(cudaStreamWaitEvent(h->h2d, h->start, 0));
+  NMG_CU(cudaStreamWaitEvent(h->d2h, h->start, 0));
+  int chunks = n / kMinChunk;
+  chunks = chunks < 1 ? 1 : (chunks > kMaxChunks ? kMaxChunks : chunks);
+  const int per = (n + chunks - 1) / chunks;
+  for (int i = 0; i < chunks; ++i) {
+    const size_t o = size_t(i) * per;
+    const int m = int(size_t(n) - o < size_t(per) ? size_t(n) - o : size_t(per));
+    if (m <= 0) break;
+    const size_t f = sizeof(float);
+    if ((s = h2d(h->pos + 3 * o, in->pos + 3 * o, 3 * f * m, h->h2d)) != NMG_OK ||
+        (s = h2d(h->wo + 3 * o, in->wo + 3 * o, 3 * f * m, h->h2d)) != NMG_OK ||
+        (s = h2d(h->nrm + 3 * o, in->normal + 3 * o, 3 * f * m, h->h2d)) != NMG_OK ||
+        (s = h2d(h->rough + o, in->roughness + o, f * m, h->h2d)) != NMG_OK ||
+        (s = h2d(h->u4 + 4 * o, u4 + 4 * o, 4 * f * m, h->h2d)) != NMG_OK)
+      return s;
+    NMG_CU(cudaEventRecord(h->in_ready[i], h->h2d));
+    NMG_CU(cudaStreamWaitEvent(st, h->in_ready[i], 0));
+    const nmg_shading din{h->pos + 3 * o, h->wo + 3 * o, h->nrm + 3 * o, h->rough + o};
+    const nmg_query_out dout{h->dir + 3 * o, h->pdf + o, out->lobe ? h->lobe + o : nullptr, nullptr,
+                             out->selection ? h->sel + o : nullptr};
+    if ((s = nmg_query(c, &din, h->u4 + 4 * o, nullptr, m, &dout, stream)) != NMG_OK) return s;
+    NMG_CU(cudaEventRecord(h->out_ready[i], st));
+    NMG_CU(cudaStreamWaitEvent(h->d2h, h->out_ready[i], 0));
+    if ((s = d2h(out->dir + 3 * o, h->dir + 3 * o, 3 * f * m, h->d2h)) != NMG_OK ||
+        (s = d2h(out->pdf + o, h->pdf + o, f * m, h->d2h)) != NMG_OK)
+      return s;
+    if (out->lobe && (s = d2h(out->lobe + o, h->lobe + o, sizeof(int) * m, h->d2h)) != NMG_OK) return s;
+    if (out->selection && (s = d2h(out->selection + o, h->sel + o, f * m, h->d2h)) != NMG_OK) return s;
+  }
+  NMG_CU(cudaEventRecord(h->done, h->d2h));
+  NMG_CU(cudaStreamWaitEvent(st, h->done, 0));
+  return NMG_OK;
+}
+
+nmg_status nmg_train_step_host(nmg_ctx* c, const float* x, const float* records, int n, double* stats,
+                               nmg_stream stream) {
+  NMG_REQUIRE(c && x && records, "NULL argument");
+  NMG_REQUIRE(n >= 0 && n <= c->ws.cap_b, "n=%d outside 0..%d (call nmg_reserve)", n, c->ws.cap_b);
+  HostIO* h = nullptr;
+  nmg_status s = host_io_get(c, &h);
+  if (s != NMG_OK) return s;
+  const int ni = c->enc.n_input, rf = c->lay.record_floats;
+  if ((s = ensure_staging_b(h, c->ws.cap_b > 1 ? c->ws.cap_b : 1, ni, rf)) != NMG_OK) return s;
+  cudaStream_t st = (cudaStream_t)stream;
+  NMG_CU(cudaEventRecord(h->start, st));
+  NMG_CU(cudaStreamWaitEvent(h->h2d, h->start, 0));
+  if ((s = h2d(h->x, x, sizeof(float) * size_t(n) * ni, h->h2d)) != NMG_OK ||
+      (s = h2d(h->rec, records, sizeof(float) * size_t(n) * rf, h->h2d)) != NMG_OK)
+    return s;
+  NMG_CU(cudaEventRecord(h->in_ready[0], h->h2d));
+  NMG_CU(cudaStreamWaitEvent(st, h->in_ready[0], 0));
+  if ((s = nmg_train_step(c, h->x, h->rec, nullptr, n, stats ? h->stats : nullptr, stream)) != NMG_OK) return s;
+  if (stats) s = d2h(stats, h->stats, 2 * sizeof(double), st);
+  return s;
+}
+
+}  // extern "C"

@@ -155,17 +155,24 @@ static nmg_status reserve(nmg_ctx* c, int max_q, int max_b) {
   max_b = max_b > w.cap_b ? max_b : w.cap_b;
   cudaDeviceSynchronize();
   free_workspace(c);
-  const int cap = max_q > max_b ? max_q : max_b;
+  // The FP32 path stores every layer's activations of a batch for its
+  // backward; the fused paths recompute them inside the training kernel and
+  // keep only the query-side input rows and raw outputs (for nmg_pdf).
+  const bool fp32 = c->cfg.path == NMG_PATH_FP32;
+  const int cap = fp32 && max_b > max_q ? max_b : max_q;
   const Layout& L = c->lay;
   const size_t capz = size_t(cap > 1 ? cap : 1);
   nmg_status s;
-#define A(p, n) \
-  if ((s = dalloc(&(p), (n))) != NMG_OK) return s;
+#define A(p, n)                                       \
+  do {                                                \
+    if ((s = dalloc(&(p), (n))) != NMG_OK) return s; \
+    w.bytes += size_t(n) * sizeof(*(p));              \
+  } while (0)
   A(w.x, capz * c->enc.n_input);
   A(w.partials, 2 * 2048);
   A(w.raw, capz * L.n_out_pad);
   w.n_partials = 2 * 2048;
-  if (c->cfg.path == NMG_PATH_FP32 || max_b > 0) {
+  if (fp32) {
     A(w.enc, capz * c->enc.n_enc_pad);
     for (int l = 0; l < L.n_layers - 1; ++l)
       if (l < 2 || max_b > 0) A(w.h[l], capz * kWidth);
@@ -318,6 +325,7 @@ nmg_status nmg_create(const nmg_config* cfg, nmg_ctx** out) {
 void nmg_destroy(nmg_ctx* c) {
   if (!c) return;
   cudaDeviceSynchronize();
+  host_io_release(c);
   free_workspace(c);
   if (c->w_inf != c->w) cudaFree(c->w_inf);
   cudaFree(c->w);
@@ -329,6 +337,16 @@ void nmg_destroy(nmg_ctx* c) {
   cudaFree(c->w16);
   cudaFree(c->w16_inf);
   delete c;
+}
+
+nmg_status nmg_device_bytes(const nmg_ctx* c, uint64_t* bytes) {
+  NMG_REQUIRE(c && bytes, "NULL argument");
+  const size_t n = size_t(c->lay.n_params);
+  size_t b = n * (sizeof(float) * 4 + sizeof(uint32_t)) + sizeof(uint32_t);  // w, grad, m, v, step counters
+  if (c->w_inf != c->w) b += n * sizeof(float);
+  if (c->w16) b += 2 * n * sizeof(uint16_t);
+  *bytes = uint64_t(b + c->ws.bytes + c->ws.fused_bytes);
+  return NMG_OK;
 }
 
 nmg_status nmg_get_info(const nmg_ctx* c, nmg_info* info) {

@@ -242,3 +242,88 @@ def train_batch(field, n, seed=7272, input_mode=1, selection=False):
     if selection:
         cols.append(np.full(n, INV_4PI))
     return featurize(q, input_mode), np.stack(cols, axis=-1).astype(np.float32)
+
+
+class TorchTrainSource:
+    """Fresh training batches drawn on the GPU from a TrainField, one per call,
+    as a renderer would record them each frame (the same distributions as
+    train_batch: 70% of positions on the 64 planes of `wavefront`, 30% uniform;
+    wi 50% from the cell's mixture, 50% uniform; radiance = density x
+    lognormal(0, 0.5); wiPdf the pdf of that draw). Returns float32 CUDA
+    tensors (inputs [n, 10], records [n, 6|7]) for input mode 1."""
+
+    def __init__(self, field, seed=7272, device="cuda", plane_seed=None):
+        import torch
+        self.torch = torch
+        self.dev = device
+        self.gen = torch.Generator(device=device)
+        self.gen.manual_seed(seed)
+        self.cells = field.cells
+        t = lambda a: torch.as_tensor(np.asarray(a, np.float64), device=device)
+        self.w, self.kap, self.mu = t(field.w), t(field.kap), t(field.mu)
+        # the planes of wavefront(n, s) come from seed s + 1: plane_seed = s + 1 puts the training
+        # records on the same surfaces as that wavefront's queries
+        prng = np.random.default_rng(seed + 1 if plane_seed is None else plane_seed)
+        pn = uniform_sphere(prng, (64,))
+        self.pn = t(pn)
+        self.off = t(np.einsum("pj,pj->p", pn, prng.random((64, 3))))
+        infl = math.sqrt(3.0) * 0.005  # the unit box inflated by 0.5% of its diagonal (train.h:173-177)
+        self.lo, self.size = -infl, 1.0 + 2.0 * infl
+
+    def _rand(self, *shape):
+        return self.torch.rand(*shape, generator=self.gen, device=self.dev, dtype=self.torch.float64)
+
+    def _sphere(self, n):
+        torch = self.torch
+        u = self._rand(n, 2)
+        z = 1.0 - 2.0 * u[:, 0]
+        r = torch.sqrt(torch.clamp(1.0 - z * z, min=0.0))
+        ph = 2.0 * math.pi * u[:, 1]
+        return torch.stack([r * torch.cos(ph), r * torch.sin(ph), z], dim=-1)
+
+    def density(self, cell, wi):
+        torch = self.torch
+        k = self.kap[cell]
+        c = (self.mu[cell] * wi[:, None, :]).sum(-1)
+        v = k * torch.exp(k * torch.clamp(c - 1.0, max=0.0)) / (2.0 * math.pi * -torch.expm1(-2.0 * k))
+        return (self.w[cell] * v).sum(-1)
+
+    def __call__(self, n, selection=False):
+        torch = self.torch
+        n_pl = int(round(0.7 * n))
+        p = self._rand(n, 3)
+        k = torch.randint(0, 64, (n_pl,), generator=self.gen, device=self.dev)
+        d = (p[:n_pl] * self.pn[k]).sum(-1) - self.off[k]
+        p[:n_pl] = torch.clamp(p[:n_pl] - d[:, None] * self.pn[k], 0.0, 1.0)
+        ci = torch.clamp((p * self.cells).long(), 0, self.cells - 1)
+        cell = (ci[:, 0] * self.cells + ci[:, 1]) * self.cells + ci[:, 2]
+        # wi from the cell's mixture: lobe by CDF, vMF by inversion
+        lobe = torch.multinomial(self.w[cell], 1, generator=self.gen).squeeze(1)
+        kap = self.kap[cell, lobe]
+        mu = self.mu[cell, lobe]
+        u = self._rand(n, 2)
+        ct = 1.0 + torch.log1p(u[:, 0] * torch.expm1(-2.0 * kap)) / kap
+        st = torch.sqrt(torch.clamp(1.0 - ct * ct, min=0.0))
+        ph = 2.0 * math.pi * u[:, 1]
+        a = torch.where(mu[:, 2:3].abs() < 0.9, torch.tensor([0.0, 0.0, 1.0], device=self.dev, dtype=torch.float64),
+                        torch.tensor([1.0, 0.0, 0.0], device=self.dev, dtype=torch.float64))
+        t1 = torch.nn.functional.normalize(torch.cross(mu, a, dim=-1), dim=-1)
+        t2 = torch.cross(mu, t1, dim=-1)
+        own = t1 * (st * torch.cos(ph))[:, None] + t2 * (st * torch.sin(ph))[:, None] + mu * ct[:, None]
+        pick = self._rand(n) < 0.5
+        wi = torch.where(pick[:, None], own, self._sphere(n))
+        wi = torch.nn.functional.normalize(wi, dim=-1)
+        dens = self.density(cell, wi)
+        L = dens * torch.exp(0.5 * torch.randn(n, generator=self.gen, device=self.dev, dtype=torch.float64))
+        th = torch.acos(torch.clamp(wi[:, 2], -1.0, 1.0))
+        phi = torch.atan2(wi[:, 1], wi[:, 0])
+        phi = torch.where(phi < 0, phi + 2.0 * math.pi, phi)
+        cols = [th, phi, 0.8 * L, L, 1.2 * L, 0.5 * dens + 0.5 * INV_4PI]
+        if selection:
+            cols.append(torch.full_like(th, INV_4PI))
+        rec = torch.stack(cols, dim=-1).float()
+        x = torch.cat([0.5 + (p - (self.lo + self.size / 2)) / self.size,
+                       (self._sphere(n) + 1.0) * 0.5,   # wo
+                       (self._sphere(n) + 1.0) * 0.5,   # normal
+                       (1.0 - torch.exp(-self._rand(n)))[:, None]], dim=1).float()
+        return x.contiguous(), rec.contiguous()
