@@ -24,14 +24,56 @@ template <bool FAST> NMG_D void xsincos(float x, float* s, float* c) {
     sincosf(x, s, c);
 }
 template <bool FAST> NMG_D float xdiv(float a, float b) { return FAST ? __fdividef(a, b) : a / b; }
+// sin/cos of an angle x in [0, 2pi]. The hardware approximation is most
+// accurate on [-pi, pi], so FAST evaluates it at x - pi and flips the signs.
+template <bool FAST> NMG_D void xsincos_2pi(float x, float* s, float* c) {
+  if (FAST) {
+    float sn, cs;
+    __sincosf(x - NMG_PI, &sn, &cs);
+    *s = -sn;
+    *c = -cs;
+  } else {
+    sincosf(x, s, c);
+  }
+}
+// sin/cos of 2 pi t for t in [0, 1] (FAST: of pi (2t - 1), then the signs).
+template <bool FAST> NMG_D void xsincos_turn(float t, float* s, float* c) {
+  if (FAST) {
+    float sn, cs;
+    __sincosf(NMG_PI * (2.f * t - 1.f), &sn, &cs);
+    *s = -sn;
+    *c = -cs;
+  } else {
+    sincosf(NMG_TWO_PI * t, s, c);
+  }
+}
+
+// sin/cos of the lobe angles theta = pi * st and phi = 2 pi * sp (st, sp the
+// logistic outputs in (0, 1)). PRECISE uses sincospi, which needs no
+// argument reduction and keeps the mean direction to an ulp; the hardware
+// approximation (FAST and not PRECISE) is off by up to ~4e-7, which a lobe
+// of concentration kappa turns into a relative pdf error of ~4e-7 kappa.
+template <bool FAST, bool PRECISE>
+NMG_D void lobe_angles(float st, float sp, float* sth, float* cth, float* sph, float* cph) {
+  if (PRECISE) {
+    sincospif(st, sth, cth);
+    sincospif(2.f * sp, sph, cph);
+  } else {
+    xsincos<FAST>(NMG_PI * st, sth, cth);
+    xsincos_turn<FAST>(sp, sph, cph);
+  }
+}
 
 // -expm1(-x) = 1 - e^{-x} for x >= 0 without cancellation: a degree-7 Taylor
 // polynomial below x = 0.5 (relative error < 3e-8), 1 - e^{-x} above.
+// Both branches are evaluated and one is selected: lanes of a warp rarely
+// agree on the side of 0.5, and a branch would run both anyway.
 template <bool FAST> NMG_D float one_minus_exp_neg(float x) {
   if (!FAST) return -expm1f(-x);
-  if (x >= 0.5f) return 1.f - __expf(-x);
-  return x * (1.f - x * (1.f / 2.f) * (1.f - x * (1.f / 3.f) * (1.f - x * (1.f / 4.f) *
-             (1.f - x * (1.f / 5.f) * (1.f - x * (1.f / 6.f) * (1.f - x * (1.f / 7.f)))))));
+  const float big = 1.f - __expf(-x);
+  const float small = x * (1.f - x * (1.f / 2.f) * (1.f - x * (1.f / 3.f) * (1.f - x * (1.f / 4.f) *
+                      (1.f - x * (1.f / 5.f) * (1.f - x * (1.f / 6.f) * (1.f - x * (1.f / 7.f)))))));
+  return x >= 0.5f ? big : small;
 }
 template <bool FAST> NMG_D f3 unit3(f3 a) {
   if (!FAST) return normalize3(a);
@@ -76,7 +118,7 @@ template <bool FAST> NMG_D float vmf_norm(float k) {
 
 // distribution.h:85-98: activation of one query's raw outputs. `raw` points
 // at 4K floats (lambda, kappa, theta, phi per lobe), 16-byte aligned.
-template <int K, bool FAST>
+template <int K, bool FAST, bool PRECISE = !FAST>
 NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
   m.total = 0.f;
 #pragma unroll
@@ -84,11 +126,8 @@ NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
     float4 r = reinterpret_cast<const float4*>(raw)[i];
     m.lam[i] = xexp<FAST>(act_exp_clamp(r.x));
     m.kap[i] = kappa_softplus ? softplus<FAST>(r.y) : xexp<FAST>(act_exp_clamp(r.y));
-    float th = NMG_PI * logistic<FAST>(r.z);
-    float ph = NMG_TWO_PI * logistic<FAST>(r.w);
     float st, ct, sp, cp;
-    xsincos<FAST>(th, &st, &ct);
-    xsincos<FAST>(ph, &sp, &cp);
+    lobe_angles<FAST, PRECISE>(logistic<FAST>(r.z), logistic<FAST>(r.w), &st, &ct, &sp, &cp);
     m.mu[i] = f3{st * cp, st * sp, ct};
     m.total += m.lam[i];
   }
@@ -108,11 +147,8 @@ NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplu
   for (int i = 0; i < K; ++i) {
     m.lam[i] = xexp<FAST>(act_exp_clamp(raw[4 * i]));
     m.kap[i] = kappa_softplus ? softplus<FAST>(raw[4 * i + 1]) : xexp<FAST>(act_exp_clamp(raw[4 * i + 1]));
-    float th = NMG_PI * logistic<FAST>(raw[4 * i + 2]);
-    float ph = NMG_TWO_PI * logistic<FAST>(raw[4 * i + 3]);
     float st, ct, sp, cp;
-    xsincos<FAST>(th, &st, &ct);
-    xsincos<FAST>(ph, &sp, &cp);
+    lobe_angles<FAST, !FAST>(logistic<FAST>(raw[4 * i + 2]), logistic<FAST>(raw[4 * i + 3]), &st, &ct, &sp, &cp);
     m.mu[i] = f3{st * cp, st * sp, ct};
     m.total += m.lam[i];
   }
@@ -208,12 +244,11 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
       mu = m.mu[i];
     }
   f3 loc;
-  float ph = NMG_TWO_PI * u1;
   float sp, cp;
   if (k < NMG_EPS) {  // render/sampling.h:32-37, then rotated like any lobe sample (vmf.h:67-71)
     float z = 1.f - 2.f * u0;
     float r = sqrtf(fmaxf(0.f, 1.f - z * z));
-    xsincos<FAST>(ph, &sp, &cp);
+    xsincos_turn<FAST>(u1, &sp, &cp);
     loc = f3{r * cp, r * sp, z};
   } else {
   // cos(theta) = 1 + log1p(-u0 + e^{-2k} u0) / k (vmf.h:51), evaluated as
@@ -232,7 +267,7 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
     s2 = opc * (2.f - opc);
   }
   float st = sqrtf(fmaxf(0.f, s2));
-  xsincos<FAST>(ph, &sp, &cp);
+  xsincos_turn<FAST>(u1, &sp, &cp);
   loc = f3{cp * st, sp * st, ct};
   }
   // Frame(mu): T = normalize(mu x e), e the branchless axis pick; B = normalize(mu x T)
@@ -277,7 +312,7 @@ NMG_D float raw_at(const float (&raw)[N], int i) { return raw[i < N ? i : 0]; }
 // dF/dlambda uses the O(K) form (vmf_s - q)/total, algebraically equal to
 // the reference's O(K^2) sum. NaN/Inf gradients become 0 and gradients are
 // clamped above at 150 (train.cu:109-123). Returns the per-sample loss.
-template <int K, bool FAST, class RAW>
+template <int K, bool FAST, bool PRECISE = !FAST, class RAW>
 NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, const MixOpts& o, float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
   float total = 0.f;
@@ -294,13 +329,12 @@ NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, cons
     }
     sgt[i] = logistic<FAST>(r.z);
     sgp[i] = logistic<FAST>(r.w);
-    xsincos<FAST>(NMG_PI * sgt[i], &sth[i], &cth[i]);
-    xsincos<FAST>(NMG_TWO_PI * sgp[i], &sph[i], &cph[i]);
+    lobe_angles<FAST, PRECISE>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
     total += lam[i];
   }
   float swt, cwt, swp, cwp;
-  xsincos<FAST>(rec[0], &swt, &cwt);
-  xsincos<FAST>(rec[1], &swp, &cwp);
+  xsincos<FAST && !PRECISE>(rec[0], &swt, &cwt);
+  xsincos_2pi<FAST && !PRECISE>(rec[1], &swp, &cwp);
   const f3 wi{swt * cwp, swt * swp, cwt};
   float vmf[K];
   float q = 0.f;
@@ -354,7 +388,7 @@ NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, cons
 // train.cu:126-172: the learned-selection variant. raw[4K] is the selection
 // logit; rec[6] the BSDF pdf of the direction. No NaN/clamp post-pass
 // (the reference has none for this variant). grad has 4K+1 entries.
-template <int K, bool FAST, class RAW>
+template <int K, bool FAST, bool PRECISE = !FAST, class RAW>
 NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float scale, const MixOpts& o,
                                        float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
@@ -372,15 +406,14 @@ NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float s
     }
     sgt[i] = logistic<FAST>(r.z);
     sgp[i] = logistic<FAST>(r.w);
-    xsincos<FAST>(NMG_PI * sgt[i], &sth[i], &cth[i]);
-    xsincos<FAST>(NMG_TWO_PI * sgp[i], &sph[i], &cph[i]);
+    lobe_angles<FAST, PRECISE>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
     total += lam[i];
   }
   const float xs = raw_at(raw, 4 * K);
   const float sel = logistic<FAST>(xs);
   float swt, cwt, swp, cwp;
-  xsincos<FAST>(rec[0], &swt, &cwt);
-  xsincos<FAST>(rec[1], &swp, &cwp);
+  xsincos<FAST && !PRECISE>(rec[0], &swt, &cwt);
+  xsincos_2pi<FAST && !PRECISE>(rec[1], &swp, &cwp);
   const f3 wi{swt * cwp, swt * swp, cwt};
   float vmf[K];
   float q = 0.f;

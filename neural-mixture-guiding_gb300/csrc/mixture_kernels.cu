@@ -27,6 +27,15 @@ nmg_status set_error(nmg_status st, const char* fmt, ...) {
 
 constexpr int kThreads = 128;
 
+// Hardware transcendental approximations (__expf, __fdividef, __sincosf for
+// the sampled azimuth): the reference compiles all of its CUDA with
+// --use_fast_math (src/backend/CMakeLists.txt:96), so its own GPU mixture
+// code evaluates the same approximations. The lobe means and the record
+// directions stay precise (sincospi / sincosf): their error is multiplied by
+// kappa in exp(kappa (cos - 1)), up to kappa = 1000 in this workload. The
+// vMF sampler keeps its accurate log1p.
+constexpr bool kMixFast = true;
+
 static int grid_for(long n) {
   long blocks = (n + kThreads - 1) / kThreads;
   long cap = 152L * 16;  // 16 resident 128-thread blocks per SM
@@ -41,7 +50,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_sample(const float* __rest
                                                              float* __restrict__ pdf, int* __restrict__ lobe) {
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
     Mix<K> m;
-    mix_activate<K, FAST>(m, raw + q * stride, kappa_softplus);
+    mix_activate<K, FAST, true>(m, raw + q * stride, kappa_softplus);
     if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
     float4 u = reinterpret_cast<const float4*>(u4)[q];
     int sel = mix_select<K>(m, u.y);
@@ -59,7 +68,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_pdf(const float* __restric
                                                           int kappa_softplus, float* __restrict__ pdf) {
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
     Mix<K> m;
-    mix_activate<K, FAST>(m, raw + q * stride, kappa_softplus);
+    mix_activate<K, FAST, true>(m, raw + q * stride, kappa_softplus);
     if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
     pdf[q] = mix_pdf<K, FAST>(m, load3(wi, q));
   }
@@ -93,8 +102,8 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad(const float* __r
 #pragma unroll
     for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
     float g[4 * K + 1];
-    float l = SEL ? mix_kl_loss_grad_selection<K, false>(raw + q * stride, r, scale, o, g)
-                  : mix_kl_loss_grad<K, false>(raw + q * stride, r, scale, o, g);
+    float l = SEL ? mix_kl_loss_grad_selection<K, kMixFast, true>(raw + q * stride, r, scale, o, g)
+                  : mix_kl_loss_grad<K, kMixFast, true>(raw + q * stride, r, scale, o, g);
     float4* gr = reinterpret_cast<float4*>(grad + q * stride);
 #pragma unroll
     for (int i = 0; i < K; ++i) gr[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
@@ -116,7 +125,7 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int m, doubl
 template <int K>
 static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, const float* u4, const float* cosn,
                                 int n, float* dir, float* pdf, int* lobe, cudaStream_t st) {
-  k_mixture_sample<K, false><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
+  k_mixture_sample<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
                                                                dir, pdf, lobe);
   return check_launch("nmg_mixture_sample");
 }
@@ -124,7 +133,7 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
 template <int K>
 static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const float* wi, const float* cosn, int n,
                              float* pdf, cudaStream_t st) {
-  k_mixture_pdf<K, false><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
+  k_mixture_pdf<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
   return check_launch("nmg_mixture_pdf");
 }
 
