@@ -38,9 +38,9 @@ N_QUERIES = 1920 * 1080
 N_TRAIN = 1 << 18
 FLOP_PER_QUERY = 2 * (80 * 64 + 64 * 64 + 64 * 64 + 64 * 48)  # 32,768 executed (padded) MLP FLOP
 BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, rough, u4 in; dir, pdf, lobe, sel out
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query launch over the same 2,073,600-query
-# wavefront (ncu capture summarised in profiles/k_fused_query_hashgrid_2073600.md)
-TRAFFIC_QUERY_BYTES = 141_467_904 + 37_670_400
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query_ws launch over the same
+# 2,073,600-query wavefront (ncu capture summarised in profiles/k_fused_query_ws_hashgrid_2073600.md)
+TRAFFIC_QUERY_BYTES = 141_327_616 + 37_800_704
 
 
 def peaks():
@@ -289,12 +289,13 @@ def run_ours(args):
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "api": "nmg_query_host + nmg_train_step_host (pinned host memory)", "final_loss": e2e_loss},
         "gpu_launches": None,
-        "roofline": {"kernel": "k_fused_query" if path != nmg.PATH_FP32 else "plain query kernels",
+        "roofline": {"kernel": "k_fused_query_ws" if path != nmg.PATH_FP32 else "plain query kernels",
                      "bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",
                      "frac": tflops / bf16, "peak_source": src,
                      "traffic": TRAFFIC_QUERY_BYTES if path == nmg.PATH_BF16 else None,
                      "traffic_unit": "bytes per launch (ncu)",
-                     "limiter": "SM issue and L2 gather latency (16 warps/SM, long_scoreboard), not HBM or tensor",
+                     "limiter": "hash-grid gathers: ~69 L2 sector requests per query, L1->L2 request path 71% busy "
+                                "(ncu), not HBM or the tensor pipe",
                      "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm,
                      "per_unit": {"flop_per_query": FLOP_PER_QUERY, "hbm_bytes_per_query": BYTES_PER_QUERY},
                      "kernel_ms": t_kernel * 1e3},

@@ -332,9 +332,15 @@ nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int 
 
 /*
  * Tiling of the fused query kernel: warpgroups (128-query tiles in flight)
- * per CTA, one CTA per SM; 0 selects the default (4). 5 and 6 are valid when
- * the padded output width is <= 64. No counterpart in the reference (its
- * FullyFusedMLP launch shape is fixed, fully_fused_mlp.cu:500-558).
+ * per CTA, one CTA per SM; 5 and 6 are valid when the padded output width is
+ * <= 64. 8-12 select configurations of the warp-specialised kernel: encoder
+ * warpgroups feed MLP + mixture warpgroups through a shared-memory ring
+ * (8: 4 + 2 warpgroups, 4 slots; 9: 5 + 1, 5 slots; 10: 6 + 2, 6 slots;
+ * 11: 4 + 2, 8 slots; 12: 4 + 2, 4 slots holding the hidden activations too).
+ * 0 selects the default: 8, or 4 for 16-lobe networks. nmg_get_query_tiling
+ * reports the tiling in use (0 on the FP32 path). No counterpart in the
+ * reference (its FullyFusedMLP launch shape is fixed,
+ * fully_fused_mlp.cu:500-558).
  */
 nmg_status nmg_set_query_tiling(nmg_ctx* ctx, int warpgroups_per_cta);
 int nmg_get_query_tiling(const nmg_ctx* ctx);

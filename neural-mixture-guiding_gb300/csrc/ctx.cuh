@@ -91,6 +91,8 @@ nmg_status fused_query(nmg_ctx* c, const nmg_shading* in, const float* u4, const
                        const nmg_query_out* out, cudaStream_t st);
 nmg_status fused_infer_raw(nmg_ctx* c, const float* x, const int* d_count, int n_max, int which, float* raw,
                            cudaStream_t st);
+nmg_status fused_pdf(nmg_ctx* c, const nmg_shading* in, const float* wi, const int* d_count, int n_max, float* pdf,
+                     cudaStream_t st);
 nmg_status pack_images(nmg_ctx* c, cudaStream_t st);
 void fused_release(nmg_ctx* c);
 nmg_status fused_check_errors(nmg_ctx* c);
@@ -98,6 +100,7 @@ nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, in
                           int use_cache, int* chosen, cudaStream_t st);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st);
+int fused_default_tiling(const nmg_ctx* c);
 
 // host_io.cu
 void host_io_release(nmg_ctx* c);

@@ -29,6 +29,7 @@ struct FusedArgs {
   const float* nrm;
   const float* rough;
   const float* u4;
+  const float* wi;                   // non-NULL: evaluate the pdf at wi[n][3] instead of sampling
   const float* x;
   const int* d_count;
   int n_max;
@@ -217,6 +218,35 @@ NMG_D void load_row(const float* x, long q, int n_input, float (&v)[10]) {
 
 NMG_D f3 face_fwd(f3 n, f3 v) { return dot3(n, v) > 0.f ? n : f3{-n.x, -n.y, -n.z}; }
 
+// Output stage of one query from its raw network outputs r (registers):
+// optional raw row, then (unless raw_mode) the mixture with the optional
+// cosine lobe, and either the sampled direction with its pdf, lobe and
+// selection probability, or (a.wi set) the pdf at the given direction.
+template <int K, int NOUTMAX>
+NMG_D void query_epilogue(const FusedArgs& a, long q, const float (&r)[NOUTMAX]) {
+  if (a.raw) {
+    float4* dst = reinterpret_cast<float4*>(a.raw + q * a.n_out_pad);
+#pragma unroll
+    for (int c = 0; c < NOUTMAX / 4; ++c)
+      if (c * 4 < a.n_out_pad) dst[c] = make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+  }
+  if (a.raw_mode) return;
+  Mix<K> m;
+  mix_activate_regs<K, true>(m, r, a.mix.kappa_softplus);
+  if (a.mix.cosine) mix_apply_cosine<K, true>(m, face_fwd(load3(a.nrm, q), load3(a.wo, q)));
+  if (a.wi) {
+    a.pdf[q] = mix_pdf<K, true>(m, load3(a.wi, q));
+    return;
+  }
+  const float4 u = reinterpret_cast<const float4*>(a.u4)[q];
+  const int sel = mix_select<K>(m, u.y);
+  const f3 dv = mix_sample_lobe<K, true>(m, sel, u.z, u.w);
+  store3(a.dir, q, dv);
+  a.pdf[q] = mix_pdf<K, true>(m, dv);
+  if (a.lobe) a.lobe[q] = sel;
+  if (a.sel && a.selection) a.sel[q] = logistic<true>(r[4 * K < NOUTMAX ? 4 * K : 0]);
+}
+
 // ------------------------------------------------------------ weight image
 struct PackArgs {
   long off[kMaxLayers + 1];
@@ -237,5 +267,13 @@ struct FusedState {
 inline FusedState* fstate(nmg_ctx* c) { return reinterpret_cast<FusedState*>(c->ws.fused); }
 
 FusedArgs fused_make_args(nmg_ctx* c, bool infer_weights);
+
+// Query tilings >= 8 select a configuration of the warp-specialised kernel
+// (fused_ws.cu): 8 = 4 encoder + 2 consumer warpgroups, 4 ring slots;
+// 9 = 5 + 1, 5 slots; 10 = 6 + 2, 6 slots; 11 = 4 + 2, 8 slots;
+// 12 = 4 + 2, 4 slots, hidden activations kept in the slot.
+constexpr int kTilingWarpSpecialised = 8;
+constexpr int kTilingLast = 12;
+nmg_status launch_query_ws(int preset, int tiling, const FusedArgs& a, cudaStream_t st);
 
 }  // namespace nmg

@@ -436,11 +436,7 @@ nmg_status nmg_pdf(nmg_ctx* c, const nmg_shading* in, const float* wi, const int
   NMG_REQUIRE(in->pos && in->wo && in->normal && in->roughness && wi && pdf, "NULL input or output");
   cudaStream_t st = (cudaStream_t)stream;
   if (c->cfg.path == NMG_PATH_FP32) return plain_pdf(c, in, wi, d_count, n_max, pdf, st);
-  s = plain_featurize(c, in, d_count, n_max, c->ws.x, st);
-  if (s != NMG_OK) return s;
-  s = fused_infer_raw(c, c->ws.x, d_count, n_max, 1, c->ws.raw, st);
-  if (s != NMG_OK) return s;
-  return pdf_from_raw(c, c->ws.raw, in, wi, d_count, n_max, pdf, st);
+  return fused_pdf(c, in, wi, d_count, n_max, pdf, st);
 }
 
 nmg_status nmg_train_step(nmg_ctx* c, const float* x, const float* records, const int* d_count, int n_max,
@@ -465,14 +461,21 @@ nmg_status nmg_network_vjp(nmg_ctx* c, const float* x, const float* draw, int n,
 
 nmg_status nmg_set_query_tiling(nmg_ctx* c, int warpgroups_per_cta) {
   NMG_REQUIRE(c != nullptr, "ctx is NULL");
-  NMG_REQUIRE(warpgroups_per_cta == 0 || (warpgroups_per_cta >= 4 && warpgroups_per_cta <= 6),
-              "warpgroups_per_cta=%d (0 = default, 4..6)", warpgroups_per_cta);
-  NMG_REQUIRE(warpgroups_per_cta <= 4 || c->lay.n_out_pad <= 64, "more than 4 warpgroups needs <= 64 outputs");
+  NMG_REQUIRE(warpgroups_per_cta == 0 || (warpgroups_per_cta >= 4 && warpgroups_per_cta <= 6) ||
+                  (warpgroups_per_cta >= 8 && warpgroups_per_cta <= 12),
+              "warpgroups_per_cta=%d (0 = default, 4..6, or 8..12 = warp-specialised)", warpgroups_per_cta);
+  NMG_REQUIRE(warpgroups_per_cta == 4 || warpgroups_per_cta == 8 || warpgroups_per_cta == 0 ||
+                  c->lay.n_out_pad <= 64,
+              "tiling %d needs <= 64 outputs", warpgroups_per_cta);
   c->query_wg = warpgroups_per_cta;
   return NMG_OK;
 }
 
-int nmg_get_query_tiling(const nmg_ctx* c) { return c ? (c->query_wg > 0 ? c->query_wg : 4) : -1; }
+int nmg_get_query_tiling(const nmg_ctx* c) {
+  if (!c) return -1;
+  if (c->query_wg > 0) return c->query_wg;
+  return c->cfg.path == NMG_PATH_FP32 ? 0 : fused_default_tiling(c);
+}
 
 nmg_status nmg_autotune_query(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
                               int use_cache, int* chosen, nmg_stream stream) {

@@ -65,6 +65,11 @@ NMG_D bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return true;
 }
 
+// Plain arrival (release at CTA scope).
+NMG_D void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
 NMG_D void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                : "memory");
@@ -151,6 +156,12 @@ NMG_D void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 NMG_D void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// Register reallocation between warpgroups (all warps of the warpgroup
+// execute it). The block's total stays what it was launched with: the
+// caller checks the kernel's launch register count before using these.
+template <int N> NMG_D void reg_dealloc() { asm volatile("setmaxnreg.dec.sync.aligned.u32 %0;" ::"n"(N)); }
+template <int N> NMG_D void reg_alloc() { asm volatile("setmaxnreg.inc.sync.aligned.u32 %0;" ::"n"(N)); }
 
 // Named barrier over `count` threads (a warpgroup = 128).
 NMG_D void bar_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }

@@ -11,6 +11,8 @@ accumulate) against the FP64 oracle.
     lobe index as the FP32 path, direction 1e-3, pdf relative 1e-3
     (+ 4e-7 kappa_max conditioning).
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -98,6 +100,38 @@ def test_fused_query_mixture(field, oracle, synth):
     if f.cfg.selection:
         sel = out["selection"].cpu().numpy()
         assert np.abs(sel - 1 / (1 + np.exp(-raw[:, 4 * K].astype(np.float64)))).max() < 1e-4
+
+
+def test_fused_pdf_at_given_directions(field, oracle, synth):
+    """nmg_pdf in one fused pass: at the query's own sampled directions it returns the query's pdf, and at
+    arbitrary directions it matches the FP64 mixture on the network's raw outputs; rows past the device
+    count stay untouched."""
+    import torch
+    f, net, fp16 = field
+    perturb(f, 4)
+    K = f.cfg.n_lobes
+    q = synth.wavefront(16384, seed=14)
+    pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
+    out = f.query(pos, wo, n, r, u4, want_raw=True)
+    p_own = f.pdf(pos, wo, n, r, out["dir"])
+    rel = ((p_own - out["pdf"]).abs() / out["pdf"]).max().item()
+    assert rel <= 1e-6, rel
+    wi = synth.uniform_sphere(np.random.default_rng(15), (16384,)).astype(np.float32)
+    p = f.pdf(pos, wo, n, r, dev(wi)[0]).cpu().numpy()
+    raw = out["raw"].cpu().numpy()
+    s = np.where((q["normal"] * q["wo"]).sum(1, keepdims=True) > 0, 1.0, -1.0).astype(np.float32)
+    p64 = oracle.mixture_pdf(raw, K, wi, (q["normal"] * s).astype(np.float32), fp64=True)
+    kmax = np.exp(np.clip(raw[:, 1:4 * K:4].astype(np.float64), -10, 15)).max(axis=1) + 2.2
+    assert np.all(np.abs(p - p64) / p64 <= 1e-3 + 4e-7 * kmax)
+    cnt = torch.tensor([5000], dtype=torch.int32, device="cuda")
+    pc = torch.full((16384,), -1.0, device="cuda")
+    wid = dev(wi)[0]
+    st = f.L.nmg_pdf(f.h, ctypes.byref(f.shading(pos, wo, n, r)), wid.data_ptr(), cnt.data_ptr(), 16384,
+                     pc.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert torch.equal(pc[:5000].cpu(), torch.from_numpy(p[:5000])) and bool((pc[5000:] == -1.0).all())
+    f.check_errors()
 
 
 def test_fused_device_count_and_ragged(field, synth):
@@ -236,7 +270,7 @@ def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
     q = synth.wavefront(50000, seed=21)
     pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
     ref = None
-    for wg in (4, 5, 6):
+    for wg in (4, 5, 6, 8, 9, 10, 11, 12):
         f.set_query_tiling(wg)
         out = f.query(pos, wo, n, r, u4, want_raw=True)
         if ref is None:
@@ -252,7 +286,7 @@ def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
             rel = (out["pdf"] - ref["pdf"])[same].abs() / ref["pdf"][same]
             assert float(rel.pow(2).mean().sqrt()) <= 1e-3, wg
     chosen = f.autotune(pos, wo, n, r, u4, use_cache=True)
-    assert chosen in (4, 5, 6) and f.query_tiling == chosen
+    assert chosen in (4, 5, 6, 8, 9, 10, 11, 12) and f.query_tiling == chosen
     assert (tmp_path / "tune.txt").read_text().strip().endswith(str(chosen))
     f.set_query_tiling(0)
     assert f.autotune(pos, wo, n, r, u4, use_cache=True) == chosen  # served from the cache
