@@ -117,8 +117,65 @@ NMG_D bool signal_ready(int g, int t, uint64_t* ready, bool ok) {
   return ok;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
-__global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __grid_constant__ TrainArgs ta) {
+// Adds one record's grid-feature gradient df[F] of level lv into the table
+// gradient gt with the corner weights of position p3 (grid.h:387-510).
+template <int F, bool SMOOTH>
+NMG_D void scatter_level(const FusedArgs& a, float* gt, int lv, const float (&p3)[3], const float (&df)[F]) {
+  float w[3];
+  uint32_t gc[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[lv], SMOOTH ? 1 : 0, &w[d], &gc[d]);
+  const float wxy[4] = {(1.f - w[0]) * (1.f - w[1]), w[0] * (1.f - w[1]), (1.f - w[0]) * w[1], w[0] * w[1]};
+  const float wz[2] = {1.f - w[2], w[2]};
+  if constexpr (F == 2) {
+    // Corners x and x+1 of a (y, z) pair often land on adjacent entries (always for dense
+    // levels, for even x on hashed ones: the x term of the hash is x itself); one 16-byte
+    // vector reduction then updates both, halving those atomics' L2 requests.
+#pragma unroll
+    for (int c = 0; c < 8; c += 2) {
+      const uint32_t yy = gc[1] + ((c >> 1) & 1), zz = gc[2] + (c >> 2);
+      const uint32_t e0 = a.enc.offset[lv] + level_index(a, lv, gc[0], yy, zz);
+      const uint32_t e1 = a.enc.offset[lv] + level_index(a, lv, gc[0] + 1u, yy, zz);
+      const float wt0 = wxy[c & 3] * wz[c >> 2], wt1 = wxy[(c + 1) & 3] * wz[c >> 2];
+      const float2 g0 = make_float2(wt0 * df[0], wt0 * df[1]), g1 = make_float2(wt1 * df[0], wt1 * df[1]);
+      if ((e0 ^ e1) == 1u) {  // entries 2m and 2m+1: one aligned 16-byte pair
+        const bool lo0 = e0 < e1;
+        atomicAdd(reinterpret_cast<float4*>(gt + size_t(lo0 ? e0 : e1) * 2),
+                  lo0 ? make_float4(g0.x, g0.y, g1.x, g1.y) : make_float4(g1.x, g1.y, g0.x, g0.y));
+      } else {
+        atomicAdd(reinterpret_cast<float2*>(gt + size_t(e0) * 2), g0);
+        atomicAdd(reinterpret_cast<float2*>(gt + size_t(e1) * 2), g1);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const float wt = wxy[c & 3] * wz[c >> 2];
+      const uint32_t e = a.enc.offset[lv] +
+                         level_index(a, lv, gc[0] + (c & 1), gc[1] + ((c >> 1) & 1), gc[2] + ((c >> 2) & 1));
+#pragma unroll
+      for (int k = 0; k < F; k += 2)
+        atomicAdd(reinterpret_cast<float2*>(gt + size_t(e) * F + k), make_float2(wt * df[k], wt * df[k + 1]));
+    }
+  }
+}
+
+// Scatter warps (SCAT): the CTA adds 7 warps (with the issuer warp they form
+// two more warpgroups) that apply each tile's grid gradient to the table
+// while the compute warpgroups move on to their next tile. A compute group
+// stages its layer-0 data gradient in its third hidden tile (dead by then,
+// rewritten only at the next tile's third forward layer) and arrives on
+// sfull; the scatter warps arrive on sempty when they have read it.
+// Registers: the 512-thread block launches at 128 per thread and moves 40
+// of them from the issuer/scatter warpgroups to the compute warpgroups.
+constexpr int kScatRegLaunch = 128, kScatRegCompute = 168, kScatRegScatter = 88;
+static_assert(2 * kRows * kScatRegCompute + 2 * kRows * kScatRegScatter == 4 * kRows * kScatRegLaunch,
+              "register split must equal the launch allocation");
+
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT>
+__global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
+    k_fused_train(const __grid_constant__ TrainArgs ta) {
+  static_assert(!SCAT || NWG == 2, "scatter warps pair with two compute warpgroups");
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
   constexpr int NGRID = LEVELS * F;
@@ -140,16 +197,21 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
   const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const bool issuer = warp == NWG * 4;
-  const int g = issuer ? 0 : threadIdx.x / kRows;
+  const bool scatter = SCAT && warp > NWG * 4;
+  const int g = (issuer || scatter) ? 0 : threadIdx.x / kRows;
   const int t = threadIdx.x % kRows;
   uint8_t* wsm = smem;
   uint8_t* A0 = smem + w_region + g * WG_BYTES;
   uint8_t* Hs = A0 + A_BYTES;  // three hidden tiles
   uint8_t* Dt = Hs + 3 * H_BYTES;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * WG_BYTES);  // [0] weights, then ready[], done[]
+  // [0] weights, then ready[], done[], sfull[], sempty[]
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * WG_BYTES);
   uint64_t* ready = bars + 1;
   uint64_t* done = bars + 1 + NWG;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + 2 * NWG);
+  uint64_t* sfull = bars + 1 + 2 * NWG;
+  uint64_t* sempty = bars + 1 + 3 * NWG;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + 4 * NWG);
+  constexpr int kScatThreads = SCAT ? 2 * kRows - 32 : 0;  // 7 warps after the issuer warp
   const bool fp16 = a.fp16 != 0;
   const int nout = a.n_out_pad;
   const int KC3 = nout / 8;
@@ -159,6 +221,8 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
     for (int i = 0; i < NWG; ++i) {
       tc::mbar_init(&ready[i], 1);
       tc::mbar_init(&done[i], 1);
+      tc::mbar_init(&sfull[i], 1);
+      tc::mbar_init(&sempty[i], SCAT ? kScatThreads : 1);
     }
     tc::fence_mbar_init();
   }
@@ -186,8 +250,8 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
   double loss_acc = 0.0;
   int cta_tiles = 0;
   for (int i = 0; i < NWG; ++i) cta_tiles += wg_tiles(ntiles, i, NWG);
-
   if (issuer) {
+    if constexpr (SCAT) tc::reg_dealloc<kScatRegScatter>();
     // ---------------------------------------------------- MMA issuer (one thread)
     if (lane == 0 && ok) {
       int remaining[NWG], step[NWG];
@@ -248,12 +312,51 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
       }
     }
     __syncwarp();
+    if constexpr (SCAT) tc::reg_alloc<kScatRegLaunch>();
+  } else if (scatter) {
+    // ------------------------------------------------------- scatter warps
+    tc::reg_dealloc<kScatRegScatter>();
+    // Tiles in the order the compute groups finish them (k-th tile of group
+    // 0, then of group 1, ...); items (level, row) with rows fastest, so a
+    // warp reads consecutive rows of the staged [feature][row] gradient.
+    const int sidx = int(threadIdx.x) - (NWG * 4 + 1) * 32;
+    float* gt = ta.grad + ta.n_mlp;
+    for (int k = 0; ok; ++k) {
+      bool any = false;
+      for (int gg = 0; gg < NWG && ok; ++gg) {
+        const int tile = blockIdx.x * NWG + gg + k * gridDim.x * NWG;
+        if (tile >= ntiles) continue;
+        any = true;
+        if (!tc::mbar_wait(&sfull[gg], uint32_t(k) & 1u)) {
+          ok = false;
+          break;
+        }
+        const float* dgs = reinterpret_cast<const float*>(smem + w_region + gg * WG_BYTES + A_BYTES + 2 * H_BYTES);
+        for (int item = sidx; item < kRows * LEVELS; item += kScatThreads) {
+          const int r = item % kRows, lv = item / kRows;
+          const long q = long(tile) * kRows + r;
+          if (q < n) {
+            const float* xr = ta.x + q * a.enc.n_input;
+            const float p3[3] = {xr[0], xr[1], xr[2]};
+            float df[F];
+#pragma unroll
+            for (int kk = 0; kk < F; ++kk) df[kk] = dgs[(F * lv + kk) * kRows + r];
+            scatter_level<F, SMOOTH>(a, gt, lv, p3, df);
+          }
+        }
+        tc::mbar_arrive(&sempty[gg]);
+      }
+      if (!any) break;
+    }
+    tc::reg_alloc<kScatRegLaunch>();
   } else {
     // ------------------------------------------------- compute warpgroup g
+    if constexpr (SCAT) tc::reg_alloc<kScatRegCompute>();
     uint32_t dph = 0;
     const uint32_t tD = tbase + g * DCOLS;
     const uint32_t lane_addr = (uint32_t((warp & 3) * 32) << 16);
     for (int tile = blockIdx.x * NWG + g; tile < ntiles; tile += gridDim.x * NWG) {
+      const int kt = (tile - (blockIdx.x * NWG + g)) / (gridDim.x * NWG);  // this group's tile number
       const long q = long(tile) * kRows + t;
       const bool valid = q < n;
       float x[10];
@@ -278,9 +381,12 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
           for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, v + 16 * c);
           tc::tmem_wait_ld();
           uint8_t* H = Hs + l * H_BYTES;
+          bool free_h = true;
+          if (SCAT && l == 2 && kt > 0)  // the scatter warps still read the previous tile's gradient here
+            free_h = tc::mbar_wait(&sempty[g], uint32_t(kt - 1) & 1u);
 #pragma unroll
           for (int c = 0; c < kWidth / 8; ++c) store_chunk_relu(H, t, c, kWidth / 8, v + 8 * c, fp16);
-          ok = signal_ready(g, t, &ready[g], fin && ok);
+          ok = signal_ready(g, t, &ready[g], fin && free_h && ok);
           if (!ok) break;
         } else {
 #pragma unroll
@@ -352,6 +458,17 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
         tc::tmem_wait_ld();
         ok = bar_red_and(1 + g, kRows, fin && ok);
         if (!ok) break;
+        if constexpr (SCAT) {
+          // hand the gradient to the scatter warps through the third hidden tile
+          float* dgs = reinterpret_cast<float*>(Hs + 2 * H_BYTES);
+          static_assert(NGRID * kRows * 4 <= H_BYTES, "grid gradient staging fits a hidden tile");
+#pragma unroll
+          for (int j = 0; j < NGRID; ++j) dgs[j * kRows + t] = dg[j] * inv_S;
+          ok = bar_red_and(1 + g, kRows, ok);
+          if (!ok) break;
+          if (t == 0) tc::mbar_arrive(&sfull[g]);
+          continue;
+        }
         // Stage the row's grid gradient in the (now idle) delta tile, column t,
         // so the level loop below can index it: [feature][row] floats.
         float* dgs = reinterpret_cast<float*>(Dt);
@@ -363,57 +480,22 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
           float* gt = ta.grad + ta.n_mlp;
 #pragma unroll 1
           for (int lv = 0; lv < LEVELS; ++lv) {
-            float w[3];
-            uint32_t gc[3];
-#pragma unroll
-            for (int d = 0; d < 3; ++d) pos_fract(p3[d], a.enc.scale[lv], SMOOTH ? 1 : 0, &w[d], &gc[d]);
             float df[F];
 #pragma unroll
             for (int k = 0; k < F; ++k) df[k] = dgs[(F * lv + k) * kRows + t];
-            const float wxy[4] = {(1.f - w[0]) * (1.f - w[1]), w[0] * (1.f - w[1]), (1.f - w[0]) * w[1], w[0] * w[1]};
-            const float wz[2] = {1.f - w[2], w[2]};
-            if constexpr (F == 2) {
-              // Corners x and x+1 of a (y, z) pair often land on adjacent entries (always for dense
-              // levels, for even x on hashed ones: the x term of the hash is x itself); one 16-byte
-              // vector reduction then updates both, halving those atomics' L2 requests.
-#pragma unroll
-              for (int c = 0; c < 8; c += 2) {
-                const uint32_t yy = gc[1] + ((c >> 1) & 1), zz = gc[2] + (c >> 2);
-                const uint32_t e0 = a.enc.offset[lv] + level_index(a, lv, gc[0], yy, zz);
-                const uint32_t e1 = a.enc.offset[lv] + level_index(a, lv, gc[0] + 1u, yy, zz);
-                const float wt0 = wxy[c & 3] * wz[c >> 2], wt1 = wxy[(c + 1) & 3] * wz[c >> 2];
-                const float2 g0 = make_float2(wt0 * df[0], wt0 * df[1]), g1 = make_float2(wt1 * df[0], wt1 * df[1]);
-                if ((e0 ^ e1) == 1u) {  // entries 2m and 2m+1: one aligned 16-byte pair
-                  const bool lo0 = e0 < e1;
-                  atomicAdd(reinterpret_cast<float4*>(gt + size_t(lo0 ? e0 : e1) * 2),
-                            lo0 ? make_float4(g0.x, g0.y, g1.x, g1.y) : make_float4(g1.x, g1.y, g0.x, g0.y));
-                } else {
-                  atomicAdd(reinterpret_cast<float2*>(gt + size_t(e0) * 2), g0);
-                  atomicAdd(reinterpret_cast<float2*>(gt + size_t(e1) * 2), g1);
-                }
-              }
-            } else {
-#pragma unroll
-              for (int c = 0; c < 8; ++c) {
-                const float wt = wxy[c & 3] * wz[c >> 2];
-                const uint32_t e = a.enc.offset[lv] +
-                                   level_index(a, lv, gc[0] + (c & 1), gc[1] + ((c >> 1) & 1), gc[2] + ((c >> 2) & 1));
-#pragma unroll
-                for (int k = 0; k < F; k += 2)
-                  atomicAdd(reinterpret_cast<float2*>(gt + size_t(e) * F + k), make_float2(wt * df[k], wt * df[k + 1]));
-              }
-            }
+            scatter_level<F, SMOOTH>(a, gt, lv, p3, df);
           }
         }
       }
     }
+    if constexpr (SCAT) tc::reg_dealloc<kScatRegLaunch>();
   }
 
   // ---- flush the CTA's weight gradients (M = 64 accumulators) to global
   tc::fence_before_sync();
   ok = __syncthreads_and(ok) != 0;
   tc::fence_after_sync();
-  if (ok && cta_tiles > 0 && !issuer) {
+  if (ok && cta_tiles > 0 && !issuer && !scatter) {
     const int row = (warp & 3) * 16 + lane;  // valid for lane < 16
     const uint32_t qaddr = uint32_t((warp & 3) * 32) << 16;
     const uint32_t cols[4] = {CW0, CW1, CW2, CW3};
@@ -440,15 +522,15 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
   if (!ok && threadIdx.x == 0) atomicExch(a.err, 3);
   // loss partial sum of this CTA
   {
-    __shared__ double red[NWG * 4 + 1];
-    double v = issuer ? 0.0 : loss_acc;
+    __shared__ double red[SCAT ? 16 : NWG * 4 + 1];
+    double v = (issuer || scatter) ? 0.0 : loss_acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
     if (lane == 0) red[warp] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0.0;
-      for (int i = 0; i < NWG * 4; ++i) s += red[i];
+      for (int i = 0; i < int(blockDim.x / 32); ++i) s += red[i];
       ta.partials[blockIdx.x] = s;
     }
   }
@@ -460,17 +542,29 @@ __global__ void __launch_bounds__(NWG * kRows + 32, 1) k_fused_train(const __gri
   }
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT>
 static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
   constexpr int DW = NOUTMAX > kWidth ? NOUTMAX : kWidth;
-  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG>;
+  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, SCAT>;
+  if constexpr (SCAT) {
+    // the register split assumes the kernel was compiled to exactly its launch registers
+    static int regs_ok = 0;
+    if (regs_ok == 0) {
+      cudaFuncAttributes attr;
+      regs_ok = cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(kern)) == cudaSuccess &&
+                        attr.numRegs == kScatRegLaunch
+                    ? 1
+                    : -1;
+    }
+    if (regs_ok < 0) return launch_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, false>(a, grid, st);
+  }
   const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) +
                       NWG * (size_t(kRows) * NENC * 2 + 3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2) + 256;
   nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
   if (s != NMG_OK) return s;
-  kern<<<grid, NWG * kRows + 32, smem, st>>>(a);
+  kern<<<grid, SCAT ? 4 * kRows : NWG * kRows + 32, smem, st>>>(a);
   return check_launch("k_fused_train");
 }
 
@@ -502,9 +596,9 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   NMG_CUDA_TRY(cudaMemsetAsync(c->ws.partials, 0, sizeof(double) * (c->ws.n_partials / 2), st));
   nmg_status r;
   switch (s->preset) {
-    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false, 2>(a, grid, st); break;
-    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false, 1>(a, grid, st); break;
-    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true, 2>(a, grid, st); break;
+    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false, 2, true>(a, grid, st); break;
+    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false>(a, grid, st); break;
+    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true, 2, true>(a, grid, st); break;
     default: return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
   }
   if (r != NMG_OK) return r;
