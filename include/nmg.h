@@ -346,6 +346,48 @@ nmg_status nmg_set_query_tiling(nmg_ctx* ctx, int warpgroups_per_cta);
 int nmg_get_query_tiling(const nmg_ctx* ctx);
 
 /*
+ * Training records of a frame from the per-pixel radiance records the
+ * integrator keeps (the GuidedPixelStateBuffer SOA: for every path depth d a
+ * RadianceRecordItem field array indexed by pixel, guideditem.soa /
+ * workqueue.h:26-67). For every training pixel (offset + stride * (i, j) over
+ * train_res, clipped to res) and every recorded non-delta vertex, appends one
+ * network input row x[..][n_input] and one record[..][record_floats]
+ * {theta, phi, L / thp * misWeight [* bsdfVal], wiPdf[, bsdfPdf]}; vertices
+ * with NaN position, direction, pdf or radiance or a zero pdf are dropped.
+ * *d_count (device) receives the number of records, which can be passed to
+ * nmg_train_step as its device count; rows beyond `capacity` are counted but
+ * not written. Record order is not deterministic (atomic append, as the
+ * reference's TrainBuffer::push).
+ * Replaces: generate_training_data (train.cu:14-67).
+ */
+#define NMG_MAX_TRAIN_DEPTH 8
+typedef struct nmg_record_arrays {
+  const float* L;           /* [pixels][3] accumulated radiance (Color) */
+  const float* thp;         /* [pixels][3] path throughput at the vertex */
+  const float* pos;         /* [pixels][3] vertex position */
+  const float* dir;         /* [pixels][2] (theta, phi) of the scattered direction */
+  const float* wi_pdf;      /* [pixels] */
+  const float* bsdf_pdf;    /* [pixels] (may be NULL without learned selection) */
+  const float* mis_weight;  /* [pixels] */
+  const unsigned char* delta; /* [pixels] bool, may be NULL (no delta lobes) */
+  const float* bsdf_val;    /* [pixels][3] (used with product sampling, may be NULL) */
+  const float* wo;          /* [pixels][2] (theta, phi) of the outgoing direction */
+  const float* normal;      /* [pixels][2] (theta, phi) of the shading normal */
+  const float* roughness;   /* [pixels] */
+} nmg_record_arrays;
+typedef struct nmg_radiance_records {
+  int max_depth;                              /* depths recorded (<= NMG_MAX_TRAIN_DEPTH) */
+  int product;                                /* 1: multiply L by bsdfVal (GUIDED_PRODUCT_SAMPLING) */
+  const unsigned* cur_depth;                  /* [pixels] vertices recorded per pixel */
+  nmg_record_arrays depth[NMG_MAX_TRAIN_DEPTH];
+} nmg_radiance_records;
+typedef struct nmg_train_pixels {
+  unsigned offset[2], stride[2], train_res[2], res[2];
+} nmg_train_pixels;
+nmg_status nmg_extract_records(nmg_ctx* ctx, const nmg_radiance_records* records, const nmg_train_pixels* pixels,
+                               int capacity, float* x, float* out_records, int* d_count, nmg_stream stream);
+
+/*
  * One frame's bounce loop as a CUDA graph. Bounce i runs the guided query of
  * its queue (device SoA `in`, uniforms u4, queue length *d_count read on the
  * device, at most n_max; d_count NULL = n_max) and then, when train_x is
@@ -400,6 +442,20 @@ nmg_status nmg_check_errors(nmg_ctx* ctx);
  * step counters, step}. */
 nmg_status nmg_save(const nmg_ctx* ctx, const char* path);
 nmg_status nmg_load(nmg_ctx* ctx, const char* path);
+
+/* Parameters in tiny-cuda-nn's Trainer snapshot format: the MessagePack
+ * encoding (nlohmann::json::to_msgpack) of the object Trainer::serialize
+ * returns, {"n_params", "params_binary", "params_type"}
+ * (src/ext/tcnn/include/tiny-cuda-nn/trainer.h:267-305). The parameter
+ * vector is the network's [MLP | grid] in the reference's layout
+ * (network.h:85-100), so weights trained by the reference load here and the
+ * reverse. Export writes the inference (EMA) parameters as "__half"
+ * (params_type 0, tcnn's network precision) or "float" (1); import accepts
+ * either, ignores an "optimizer" entry and sets both parameter copies
+ * (resetting Adam, as nmg_set_params). No reference call site: the
+ * reference saves no networks. */
+nmg_status nmg_export_tcnn(const nmg_ctx* ctx, const char* path, int params_type);
+nmg_status nmg_import_tcnn(nmg_ctx* ctx, const char* path, nmg_stream stream);
 
 #ifdef __cplusplus
 }

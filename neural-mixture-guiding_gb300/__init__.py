@@ -161,6 +161,23 @@ class Bounce(C.Structure):
                 ("train_count", C.c_void_p), ("train_n_max", C.c_int), ("stats", C.c_void_p)]
 
 
+class RecordArrays(C.Structure):
+    _fields_ = [(name, C.c_void_p) for name in ("L", "thp", "pos", "dir", "wi_pdf", "bsdf_pdf", "mis_weight", "delta",
+                                               "bsdf_val", "wo", "normal", "roughness")]
+
+
+MAX_TRAIN_DEPTH = 8
+
+
+class RadianceRecords(C.Structure):
+    _fields_ = [("max_depth", C.c_int), ("product", C.c_int), ("cur_depth", C.c_void_p),
+                ("depth", RecordArrays * MAX_TRAIN_DEPTH)]
+
+
+class TrainPixels(C.Structure):
+    _fields_ = [("offset", C.c_uint * 2), ("stride", C.c_uint * 2), ("train_res", C.c_uint * 2), ("res", C.c_uint * 2)]
+
+
 def _bind_field(L):
     P = C.c_void_p
     sig = {
@@ -188,6 +205,9 @@ def _bind_field(L):
         "nmg_autotune_query": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), C.c_int, C.POINTER(C.c_int), P],
         "nmg_check_errors": [P],
         "nmg_save": [P, C.c_char_p],
+        "nmg_export_tcnn": [P, C.c_char_p, C.c_int],
+        "nmg_extract_records": [P, C.POINTER(RadianceRecords), C.POINTER(TrainPixels), C.c_int, P, P, P, P],
+        "nmg_import_tcnn": [P, C.c_char_p, P],
         "nmg_load": [P, C.c_char_p],
     }
     for name, args in sig.items():
@@ -419,6 +439,36 @@ class GuidingField:
 
     def check_errors(self):
         check(self.L.nmg_check_errors(self.h))
+
+    def extract_records(self, records, cur_depth, offset, stride, train_res, res, capacity, product=True,
+                        stream=None):
+        """nmg_extract_records: records = list (one per depth) of dicts of device tensors (L, thp, pos, dir,
+        wi_pdf, bsdf_pdf, mis_weight, delta (uint8), bsdf_val, wo, normal, roughness). Returns
+        (x [capacity, n_input], records [capacity, record_floats], count (device int32 [1]))."""
+        import torch
+        r = RadianceRecords()
+        r.max_depth = len(records)
+        r.product = int(product)
+        r.cur_depth = cur_depth.data_ptr()
+        for d, arrays in enumerate(records):
+            for name, _ in RecordArrays._fields_:
+                t = arrays.get(name)
+                setattr(r.depth[d], name, t.data_ptr() if t is not None else None)
+        tp = TrainPixels((C.c_uint * 2)(*offset), (C.c_uint * 2)(*stride), (C.c_uint * 2)(*train_res),
+                         (C.c_uint * 2)(*res))
+        x = torch.zeros((capacity, self.info.n_input), device="cuda")
+        rec = torch.zeros((capacity, self.info.record_floats), device="cuda")
+        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        check(self.L.nmg_extract_records(self.h, C.byref(r), C.byref(tp), int(capacity), _ptr(x), _ptr(rec),
+                                         _ptr(cnt), _stream(stream)))
+        return x, rec, cnt
+
+    def export_tcnn(self, path, params_type="__half"):
+        """Inference parameters as a tiny-cuda-nn Trainer snapshot (MessagePack)."""
+        check(self.L.nmg_export_tcnn(self.h, str(path).encode(), {"__half": 0, "float": 1}[params_type]))
+
+    def import_tcnn(self, path, stream=None):
+        check(self.L.nmg_import_tcnn(self.h, str(path).encode(), _stream(stream)))
 
     def save(self, path):
         check(self.L.nmg_save(self.h, path.encode()))

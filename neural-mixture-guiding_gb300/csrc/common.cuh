@@ -7,6 +7,7 @@
 
 #define NMG_PI 3.14159265358979323846f
 #define NMG_TWO_PI 6.28318530717958647693f
+#define NMG_INV_PI 0.318309886183790671538f
 #define NMG_INV_2PI 0.15915494309189533577f
 #define NMG_INV_4PI 0.07957747154594766788f
 #define NMG_EPS 1e-5f

@@ -211,3 +211,56 @@ def ref_loss_grad(raw, samples, loss_scale=128.0):
     loss = np.zeros(n, np.float32)
     ref_lib().ref_loss_grad(_p(raw), raw.shape[1], n, _p(samples), float(loss_scale), _p(g), _p(loss))
     return g, loss
+
+
+def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_mode=0, product=True,
+                    selection=False):
+    """Training records from per-pixel radiance records, restating the
+    reference's generate_training_data (src/render/guided/train.cu:14-67) with
+    normalizeSpatialCoord (train.h:173-177) in FP64 numpy.
+
+    rec: dict of per-depth arrays [depth][pixels(, c)]: L, thp, pos, bsdf_val
+    (3 channels), dir, wo, normal (2 angles), wi_pdf, bsdf_pdf, mis_weight,
+    roughness, delta. Returns (x [n, 9|10], records [n, 6|7]) in the
+    reference's loop order (training pixel, then depth)."""
+    aabb = np.asarray(aabb, np.float64)
+    mn, mx = aabb[:3], aabb[3:]
+    infl = np.linalg.norm(mx - mn) * 0.005  # AABB::inflate by diagonal * 0.005
+    lo, hi = mn - infl, mx + infl
+    xs, outs = [], []
+    for ty in range(train_res[1]):
+        for tx in range(train_res[0]):
+            px, py = tx * stride[0] + offset[0], ty * stride[1] + offset[1]
+            if px >= res[0] or py >= res[1]:
+                continue
+            pid = px + py * res[0]
+            for d in range(min(int(cur_depth[pid]), len(rec["L"]))):
+                if rec["delta"][d][pid]:
+                    continue
+                pos = rec["pos"][d][pid].astype(np.float64)
+                p = 0.5 + (pos - (lo + hi) / 2) / (hi - lo)
+                th, ph = rec["wo"][d][pid].astype(np.float64)
+                wo = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
+                nt, npf = rec["normal"][d][pid].astype(np.float64)
+                r = float(rec["roughness"][d][pid])
+                if input_mode == 0:
+                    aux = [nt / np.pi, npf / (2 * np.pi), 1 - np.exp(-r)]
+                else:
+                    n3 = np.array([np.sin(nt) * np.cos(npf), np.sin(nt) * np.sin(npf), np.cos(nt)])
+                    aux = list((n3 + 1) / 2) + [1 - np.exp(-r)]
+                thp = rec["thp"][d][pid].astype(np.float64)
+                L = np.where(thp > 1e-5, rec["L"][d][pid].astype(np.float64) / np.where(thp > 1e-5, thp, 1), 0.0)
+                L = L * float(rec["mis_weight"][d][pid])
+                if product:
+                    L = L * rec["bsdf_val"][d][pid].astype(np.float64)
+                direc = rec["dir"][d][pid].astype(np.float64)
+                wi_pdf = float(rec["wi_pdf"][d][pid])
+                if np.isnan(pos).any() or np.isnan(direc).any() or np.isnan(wi_pdf) or wi_pdf == 0 or np.isnan(L).any():
+                    continue
+                xs.append(np.concatenate([p, (wo + 1) / 2, aux]))
+                o = [direc[0], direc[1], L[0], L[1], L[2], wi_pdf]
+                if selection:
+                    o.append(float(rec["bsdf_pdf"][d][pid]))
+                outs.append(o)
+    ni = 9 if input_mode == 0 else 10
+    return (np.array(xs, np.float64).reshape(-1, ni), np.array(outs, np.float64).reshape(-1, 7 if selection else 6))

@@ -197,3 +197,69 @@ def test_capacity_and_argument_errors(nmg, synth):
         nmg.GuidingField(nmg.config(nmg.PRESET_REFERENCE, n_lobes=5))
     f.close()
     torch.cuda.synchronize()
+
+
+def _read_msgpack_map(buf):
+    """Just enough MessagePack to read a tcnn snapshot: a map of str keys to uint / str / bin values."""
+    pos = 0
+
+    def take(n):
+        nonlocal pos
+        out = buf[pos:pos + n]
+        pos += n
+        return out
+
+    def value():
+        t = take(1)[0]
+        if t < 0x80:
+            return t
+        if 0xa0 <= t <= 0xbf:
+            return take(t & 0x1f).decode()
+        if t in (0xcc, 0xcd, 0xce, 0xcf):
+            return int.from_bytes(take({0xcc: 1, 0xcd: 2, 0xce: 4, 0xcf: 8}[t]), "big")
+        if t in (0xc4, 0xc5, 0xc6):
+            return bytes(take(int.from_bytes(take({0xc4: 1, 0xc5: 2, 0xc6: 4}[t]), "big")))
+        if t == 0xd9:
+            return take(take(1)[0]).decode()
+        raise ValueError(hex(t))
+
+    t = take(1)[0]
+    assert 0x80 <= t <= 0x8f
+    out = {}
+    for _ in range(t & 0x0f):
+        k = value()
+        out[k] = value()
+    assert pos == len(buf)
+    return out
+
+
+def test_tcnn_snapshot_roundtrip(field, nmg, tmp_path):
+    """tiny-cuda-nn Trainer snapshot (MessagePack of {n_params, params_binary, params_type}): the file
+    holds the inference parameters in the reference's [MLP | grid] order; float snapshots restore them
+    exactly, __half snapshots to their binary16 rounding; sizes and types are checked."""
+    import torch
+    f, _ = field
+    p = f.get_params(0)
+    g = torch.Generator(device="cuda").manual_seed(31)
+    f.set_params(p + 0.05 * torch.randn(p.numel(), device="cuda", generator=g))
+    want = f.get_params(1).cpu().numpy()
+    for kind in ("float", "__half"):
+        path = tmp_path / ("snap_%s.msgpack" % kind)
+        f.export_tcnn(path, kind)
+        obj = _read_msgpack_map(path.read_bytes())
+        assert set(obj) == {"n_params", "params_binary", "params_type"}
+        assert obj["n_params"] == f.n_params and obj["params_type"] == kind
+        blob = np.frombuffer(obj["params_binary"], dtype=np.float32 if kind == "float" else np.float16)
+        expect = want if kind == "float" else want.astype(np.float16)
+        assert blob.shape == (f.n_params,) and np.array_equal(blob, expect)
+        g2 = nmg.GuidingField(f.cfg)
+        g2.import_tcnn(path)
+        for which in (0, 1):
+            assert np.array_equal(g2.get_params(which).cpu().numpy(), expect.astype(np.float32))
+        g2.close()
+    # a snapshot of another network is refused
+    other = nmg.GuidingField(nmg.config(1 - int(f.cfg.input_mode), path=nmg.PATH_FP32))
+    other.export_tcnn(tmp_path / "other.msgpack")
+    with pytest.raises(nmg.NMGError):
+        f.import_tcnn(tmp_path / "other.msgpack")
+    other.close()

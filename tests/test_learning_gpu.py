@@ -7,15 +7,18 @@ batch of 2^18 records from it on the GPU, as a renderer records new paths
 each frame (50% of directions from the field, 50% uniform; radiance =
 density x lognormal(0, 0.5)), on the same 64 planes as the evaluation
 queries. Network: the hash-grid preset with 8 lobes, no learned selection,
-Adam at learning rate 3e-3.
+Adam at learning rate 1e-3 for 3,000 steps.
 
 At the reference's 1e-2 (common/configs/nn/base.json) the bias-free MLP can
 drive every kappa logit far below the exp clamp within a few dozen steps,
 after which the guide stays at the uniform density: with the same data this
 happens or not depending on the seed, in every path (FP32, BF16, FP16) and
 in an FP64 autograd model of the same network alike. At 1e-2 a precision
-comparison therefore measures the chance of that collapse; 3e-3 learns
-steadily in every path.
+comparison therefore measures the chance of that collapse. At 3e-3 the
+float-atomic order alone moves the KL after 1,000-3,000 steps by 1-4%
+between two runs of the same path; at 1e-3 two runs agree within 0.3%
+(measured KL after 3,000 steps: FP32 0.684 / 0.683, BF16 0.660 / 0.659,
+FP16 0.673).
 
 The quality measure is KL(g || q) = E_{w~g}[log g(w) - log q(w)] per query,
 estimated on held-out queries by sampling w from the ground truth g, with q
@@ -34,9 +37,9 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-STEPS = 1000
+STEPS = 3000
 BATCH = 1 << 18
-LR = 3e-3
+LR = 1e-3
 N_EVAL = 1 << 16
 EVAL_SEED = 99
 
@@ -99,9 +102,7 @@ def test_trained_guide_beats_proposals_without_network(nmg, synth, fp32_run):
 @pytest.mark.parametrize("path", ["bf16", "fp16"])
 def test_reduced_precision_converges_like_fp32(nmg, synth, fp32_run, path):
     """Same initialisation, data and steps: the fused BF16 (FP16) path's final KL is at most 2% above
-    the plain FP32 path's. Rounding sends the paths along different trajectories, which end a few
-    per cent apart in either direction (measured: BF16 2.7% below, FP16 0.6% above), so below is
-    bounded only loosely."""
+    the plain FP32 path's (measured: 3.5% / 1.6% below it), and not implausibly far below."""
     f, gt = _train(nmg, synth, {"bf16": nmg.PATH_BF16, "fp16": nmg.PATH_FP16}[path])
     kl, kl_u, _ = _eval_kl(synth, f, gt)
     kl32 = fp32_run[0]
