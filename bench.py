@@ -211,8 +211,9 @@ def run_ours(args):
     f = ours["field"]
     hq = {k: torch.from_numpy(np.ascontiguousarray(v)).pin_memory() for k, v in q.items()}
     hx, hrec = torch.from_numpy(x).pin_memory(), torch.from_numpy(rec).pin_memory()
+    # the query's results an integrator consumes: direction, pdf and (learned selection) the selection
+    # probability; the lobe index is diagnostic and stays on the device
     hout = {"dir": torch.empty((N_QUERIES, 3)).pin_memory(), "pdf": torch.empty(N_QUERIES).pin_memory(),
-            "lobe": torch.empty(N_QUERIES, dtype=torch.int32).pin_memory(),
             "selection": torch.empty(N_QUERIES).pin_memory()}
     hstats = torch.empty(2, dtype=torch.float64).pin_memory()
     h2d = sum(t.numel() * t.element_size() for k, t in hq.items() if k != "aabb") + hx.numel() * 4 + hrec.numel() * 4

@@ -301,17 +301,21 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
 /*
  * nmg_query and nmg_train_step on HOST buffers (pinned memory gives the
  * overlap; pageable memory works but copies synchronously). nmg_query_host
- * splits the wavefront into up to 4 chunks of at least 2^19 queries and
+ * splits the wavefront into up to 8 chunks of at least 2^18 queries and
  * pipelines them over three streams: inputs of chunk i+1 go to the device
  * while chunk i is computed on `stream` and the outputs of chunk i-1 come
  * back. Every input and output array (all of in, u4, out->dir, out->pdf and,
  * when non-NULL, out->lobe and out->selection) is host memory; out->raw must
  * be NULL. nmg_train_step_host copies x and records to the device and runs
  * the step; stats (may be NULL) is HOST memory receiving the two FP64
- * statistics. Both are ordered after the work already on `stream`, and
- * `stream` waits for their last copy; the host buffers must stay valid until
- * then. The first call allocates device staging of the reserved capacity
- * (not capturable); later calls allocate nothing.
+ * statistics. Their kernels run on `stream` after the work already queued
+ * there and `stream` waits for their last copy; the input copies start as
+ * soon as the previous call's kernels have read the device staging, so they
+ * overlap other work still running on `stream` (the host input arrays must
+ * therefore be filled before the call, and all host buffers stay valid
+ * until `stream` reaches the call's end). The first call allocates device
+ * staging of the reserved capacity (not capturable); later calls allocate
+ * nothing.
  * Replaces: the host side of the reference's inference/training calls, which
  * copy nothing themselves (integrator.cpp:627-701 operate on device queues);
  * no reference counterpart as an entry point.

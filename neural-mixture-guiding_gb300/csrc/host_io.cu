@@ -8,11 +8,14 @@
 // chunk i is computed and chunk i-1's outputs go device->host. With pinned
 // host buffers the copies overlap the fused kernel almost entirely.
 //
-// Ordering with the caller's stream: everything starts after the work already
-// queued on `stream` and `stream` waits for the last output copy, so the
-// calls behave like one asynchronous operation on `stream`. The device
-// staging buffers are allocated on the first call (sized to the reserved
-// capacity) and reused; that first call is therefore not capturable.
+// Ordering: the kernels run on the caller's stream after the work already
+// queued there, and `stream` waits for the last output copy. The input
+// copies only wait until the previous call's kernels have consumed the
+// staging buffers, so they overlap whatever else the stream is still running
+// (a training step queued after the previous query, for instance): the host
+// input arrays must be ready when the call is made. The device staging
+// buffers are allocated on the first call (sized to the reserved capacity)
+// and reused; that first call is therefore not capturable.
 #include <string.h>
 
 #include <new>
@@ -22,12 +25,17 @@
 
 namespace nmg {
 
-constexpr int kMaxChunks = 4;
-constexpr int kMinChunk = 1 << 19;  // queries; smaller chunks leave the persistent grid underfilled
+// The first chunk's inputs and the last chunk's outputs cannot overlap a
+// kernel, so more, smaller chunks shorten that exposed copy time; below about
+// 2^18 queries a chunk leaves the persistent grid underfilled.
+constexpr int kMaxChunks = 8;
+constexpr int kMinChunk = 1 << 18;
 
 struct HostIO {
   cudaStream_t h2d = nullptr, d2h = nullptr;
   cudaEvent_t start = nullptr, done = nullptr;
+  // recorded after the kernels that read the query / training input staging
+  cudaEvent_t q_consumed = nullptr, t_consumed = nullptr;
   cudaEvent_t in_ready[kMaxChunks] = {}, out_ready[kMaxChunks] = {};
   int cap_q = 0, cap_b = 0;
   // query staging (SoA, device)
@@ -65,6 +73,8 @@ void host_io_release(nmg_ctx* c) {
   if (h->d2h) cudaStreamDestroy(h->d2h);
   if (h->start) cudaEventDestroy(h->start);
   if (h->done) cudaEventDestroy(h->done);
+  if (h->q_consumed) cudaEventDestroy(h->q_consumed);
+  if (h->t_consumed) cudaEventDestroy(h->t_consumed);
   for (int i = 0; i < kMaxChunks; ++i) {
     if (h->in_ready[i]) cudaEventDestroy(h->in_ready[i]);
     if (h->out_ready[i]) cudaEventDestroy(h->out_ready[i]);
@@ -83,7 +93,9 @@ static nmg_status host_io_get(nmg_ctx* c, HostIO** out) {
     bool ok = cudaStreamCreateWithFlags(&h->h2d, cudaStreamNonBlocking) == cudaSuccess &&
               cudaStreamCreateWithFlags(&h->d2h, cudaStreamNonBlocking) == cudaSuccess &&
               cudaEventCreateWithFlags(&h->start, ef) == cudaSuccess &&
-              cudaEventCreateWithFlags(&h->done, ef) == cudaSuccess;
+              cudaEventCreateWithFlags(&h->done, ef) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h->q_consumed, ef) == cudaSuccess &&
+              cudaEventCreateWithFlags(&h->t_consumed, ef) == cudaSuccess;
     for (int i = 0; ok && i < kMaxChunks; ++i)
       ok = cudaEventCreateWithFlags(&h->in_ready[i], ef) == cudaSuccess &&
            cudaEventCreateWithFlags(&h->out_ready[i], ef) == cudaSuccess;
@@ -163,8 +175,10 @@ nmg_status nmg_query_host(nmg_ctx* c, const nmg_shading* in, const float* u4, in
   if (s != NMG_OK) return s;
   if ((s = ensure_staging_q(h, c->ws.cap_q)) != NMG_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
+  // inputs: only after the previous call's kernels have read the staging (an
+  // event never recorded yet is complete); outputs: after the stream's work
+  NMG_CU(cudaStreamWaitEvent(h->h2d, h->q_consumed, 0));
   NMG_CU(cudaEventRecord(h->start, st));
-  NMG_CU(cudaStreamWaitEvent(h->h2d, h->start, 0));
   NMG_CU(cudaStreamWaitEvent(h->d2h, h->start, 0));
   int chunks = n / kMinChunk;
   chunks = chunks < 1 ? 1 : (chunks > kMaxChunks ? kMaxChunks : chunks);
@@ -194,6 +208,7 @@ nmg_status nmg_query_host(nmg_ctx* c, const nmg_shading* in, const float* u4, in
     if (out->lobe && (s = d2h(out->lobe + o, h->lobe + o, sizeof(int) * m, h->d2h)) != NMG_OK) return s;
     if (out->selection && (s = d2h(out->selection + o, h->sel + o, f * m, h->d2h)) != NMG_OK) return s;
   }
+  NMG_CU(cudaEventRecord(h->q_consumed, st));
   NMG_CU(cudaEventRecord(h->done, h->d2h));
   NMG_CU(cudaStreamWaitEvent(st, h->done, 0));
   return NMG_OK;
@@ -209,14 +224,14 @@ nmg_status nmg_train_step_host(nmg_ctx* c, const float* x, const float* records,
   const int ni = c->enc.n_input, rf = c->lay.record_floats;
   if ((s = ensure_staging_b(h, c->ws.cap_b > 1 ? c->ws.cap_b : 1, ni, rf)) != NMG_OK) return s;
   cudaStream_t st = (cudaStream_t)stream;
-  NMG_CU(cudaEventRecord(h->start, st));
-  NMG_CU(cudaStreamWaitEvent(h->h2d, h->start, 0));
+  NMG_CU(cudaStreamWaitEvent(h->h2d, h->t_consumed, 0));
   if ((s = h2d(h->x, x, sizeof(float) * size_t(n) * ni, h->h2d)) != NMG_OK ||
       (s = h2d(h->rec, records, sizeof(float) * size_t(n) * rf, h->h2d)) != NMG_OK)
     return s;
   NMG_CU(cudaEventRecord(h->in_ready[0], h->h2d));
   NMG_CU(cudaStreamWaitEvent(st, h->in_ready[0], 0));
   if ((s = nmg_train_step(c, h->x, h->rec, nullptr, n, stats ? h->stats : nullptr, stream)) != NMG_OK) return s;
+  NMG_CU(cudaEventRecord(h->t_consumed, st));
   if (stats) s = d2h(stats, h->stats, 2 * sizeof(double), st);
   return s;
 }

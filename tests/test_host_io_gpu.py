@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 @pytest.mark.parametrize("path", [1, 0])
 def test_query_host_matches_device_query(nmg, synth, path):
     import torch
-    n = 1_100_001  # two chunks, the second ragged
+    n = 1_100_001  # four chunks, the last ragged
     f = nmg.GuidingField(nmg.config(1, path=path), max_queries=n)
     q = synth.wavefront(n, seed=404)
     keys = ("pos", "wo", "normal", "rough", "u4")
@@ -57,3 +57,37 @@ def test_train_step_host_matches_device_step(nmg, synth, path):
     for g in (a, b):
         g.check_errors()
         g.close()
+
+
+def test_host_steps_interleaved_match_device_steps(nmg, synth):
+    """Alternating host-buffer training steps and queries, each on new inputs (so a copy that overtook
+    the previous kernel's use of the staging would feed stale data): the results follow the device-buffer
+    calls on the same inputs, up to the float-atomic order of the training steps."""
+    import torch
+    n, nb = 600_000, 40_000
+    keys = ("pos", "wo", "normal", "rough", "u4")
+    a = nmg.GuidingField(nmg.config(1, path=1), max_queries=n, max_batch=nb)
+    b = nmg.GuidingField(nmg.config(1, path=1), max_queries=n, max_batch=nb)
+    gt = synth.TrainField(seed=50)
+    outs = []
+    for it in range(3):
+        q = synth.wavefront(n, seed=51 + it)
+        x, rec = synth.train_batch(gt, nb, seed=61 + it, input_mode=1, selection=True)
+        hq = {k: torch.from_numpy(np.ascontiguousarray(q[k])).pin_memory() for k in keys}
+        hx, hr = torch.from_numpy(x).pin_memory(), torch.from_numpy(rec).pin_memory()
+        a.train_step_host(hx, hr)
+        ho = {"dir": torch.empty((n, 3)).pin_memory(), "pdf": torch.empty(n).pin_memory(),
+              "lobe": torch.empty(n, dtype=torch.int32).pin_memory()}
+        a.query_host(*(hq[k] for k in keys), ho)
+        b.train_step(hx.cuda(), hr.cuda())
+        ref = b.query(*(hq[k].cuda() for k in keys))
+        outs.append((ho, ref))
+    torch.cuda.synchronize()
+    for ho, ref in outs:
+        same = ho["lobe"] == ref["lobe"].cpu()
+        assert float(same.float().mean()) >= 0.999
+        rel = ((ho["pdf"] - ref["pdf"].cpu()) / ref["pdf"].cpu())[same]
+        assert float(rel.pow(2).mean().sqrt()) <= 1e-3
+    a.check_errors()
+    for f in (a, b):
+        f.close()
