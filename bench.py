@@ -205,6 +205,7 @@ def run_ours(args):
     ours = measure(path, args.steps, args.warmup, Clocks())
     plain = measure(nmg.PATH_FP32, max(1, min(args.steps, 3)), 1) if path != nmg.PATH_FP32 else ours
     frame = frame_graph(nmg, synth, torch, np, dx, drec, path) if path != nmg.PATH_FP32 and not args.no_frame else None
+    mix = mixture_kernels(nmg, synth, torch, flush, peaks()[0])
 
     # end to end through the public API on host buffers (nmg_query_host / nmg_train_step_host): pinned host
     # inputs in, host results out, every step; the library pipelines the copies with the kernels
@@ -303,6 +304,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "clocks": ours["clocks"],
         "frame_graph": frame,
+        "mixture_kernels": mix,
     }
     line["gpu_launches"] = launches_per_step(path) * steps
     print(json.dumps(line), flush=True)
@@ -359,6 +361,53 @@ def frame_graph(nmg, synth, torch, np, dx, drec, path, lobes=(8, 16), frames=5, 
         fr.close()
         f.close()
     return res
+
+
+def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
+    """The mixture-only workload (K = 8 raw outputs per query, no network) at the size SURVEY-style
+    bandwidth figures use, 2^21 queries: sample+pdf and KL loss+gradient, CUDA events, L2 flushed.
+    Algorithmic bytes per query: 164 (raw 128 + uniforms 16 in; direction 12, pdf 4, lobe 4 out) and
+    284 (raw 128 + record 28 in; gradient 128 out)."""
+    raw, u4, rec = synth.mixture_batch(n, K, seed=7272, selection=False)
+    r, u, rc = (torch.from_numpy(a).cuda() for a in (raw, u4, rec))
+    d = torch.empty((n, 3), device="cuda")
+    p = torch.empty(n, device="cuda")
+    lb = torch.empty(n, device="cuda", dtype=torch.int32)
+    g = torch.empty_like(r)
+    lib = nmg.lib()
+    opts = nmg.mixture_opts(K, r.shape[1])
+    ws_bytes = lib.nmg_mixture_loss_workspace_bytes(n)
+    ws = torch.empty(max(ws_bytes, 16), dtype=torch.uint8, device="cuda")
+    tot = torch.empty(1, dtype=torch.float64, device="cuda")
+    st = torch.cuda.current_stream()
+    ptr = lambda t: ctypes.c_void_p(t.data_ptr())
+
+    def sample():
+        nmg.check(lib.nmg_mixture_sample(ctypes.byref(opts), ptr(r), ptr(u), None, n, ptr(d), ptr(p), ptr(lb),
+                                         ctypes.c_void_p(st.cuda_stream)))
+
+    def loss():
+        nmg.check(lib.nmg_mixture_loss_grad(ctypes.byref(opts), ptr(r), ptr(rc), rc.shape[1], n, ctypes.c_float(128.0),
+                                            ptr(g), None, ptr(tot), ptr(ws), ctypes.c_size_t(ws_bytes),
+                                            ctypes.c_void_p(st.cuda_stream)))
+
+    out = {"queries": n, "K": K, "l2": "flushed (256 MiB write) before each timed launch"}
+    for name, fn, per in (("sample_pdf", sample, 164), ("loss_grad", loss, 284)):
+        for _ in range(3):
+            fn()
+        ts = []
+        for i in range(reps):
+            flush.fill_(i)
+            a, b = torch.cuda.Event(True), torch.cuda.Event(True)
+            a.record(st)
+            fn()
+            b.record(st)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        t = sorted(ts)[reps // 2]
+        gbs = per * n / t / 1e9
+        out[name] = {"us": t * 1e6, "bytes_per_query": per, "achieved_gbs": gbs, "hbm_frac": gbs / hbm}
+    return out
 
 
 def launches_per_step(path):

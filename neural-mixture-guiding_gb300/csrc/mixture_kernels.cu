@@ -122,9 +122,162 @@ __global__ void k_sum_partials(const double* __restrict__ partials, int m, doubl
   if (threadIdx.x == 0) *out = s;
 }
 
+// ---------------------------------------------------------------------------
+// Two threads per query (even K): lanes 2j and 2j+1 of a warp hold lobes
+// [0, K/2) and [K/2, K) of query j and combine their partial sums with pair
+// shuffles. Half the lobes per thread halves the registers that pin the
+// occupancy of the one-thread-per-query kernels, and a warp's 128-bit loads
+// cover 16 whole contiguous rows. Sums over all lobes (weights, pdf, loss)
+// add the two halves' partial sums.
+NMG_D unsigned pair_mask() { return 3u << ((threadIdx.x & 31) & ~1u); }
+NMG_D float pair_sum(float v) { return v + __shfl_xor_sync(pair_mask(), v, 1); }
+
+// Weights from the pair's total (after activation or the cosine product).
+template <int KH, bool FAST>
+NMG_D void pair_weights(Mix<KH>& m, float total) {
+  m.total = total;
+  const float inv = 1.f / total;
+#pragma unroll
+  for (int i = 0; i < KH; ++i) m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / total;
+}
+
+template <int K, bool FAST>
+NMG_D void pair_mixture(Mix<K / 2>& m, const float* row, const float* cosn, long q, int h, int kappa_softplus) {
+  constexpr int KH = K / 2;
+  mix_activate<KH, FAST, true>(m, row + h * KH * 4, kappa_softplus);
+  float lt = 0.f;
+#pragma unroll
+  for (int i = 0; i < KH; ++i) lt += m.lam[i];
+  pair_weights<KH, FAST>(m, pair_sum(lt));
+  if (cosn) {
+    mix_apply_cosine<KH, FAST>(m, load3(cosn, q));
+    lt = 0.f;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) lt += m.lam[i];
+    pair_weights<KH, FAST>(m, fmaxf(pair_sum(lt), NMG_EPS));  // distribution.h:191
+  }
+}
+
+template <int K, bool FAST>
+__global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restrict__ raw, int stride,
+                                                           const float* __restrict__ wi,
+                                                           const float* __restrict__ cosn, int n,
+                                                           int kappa_softplus, float* __restrict__ pdf) {
+  constexpr int KH = K / 2;
+  const int h = threadIdx.x & 1;
+  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += long(gridDim.x) * blockDim.x) {
+    const long q = t >> 1;
+    Mix<KH> m;
+    pair_mixture<K, FAST>(m, raw + q * stride, cosn, q, h, kappa_softplus);
+    const float p = pair_sum(mix_pdf<KH, FAST>(m, load3(wi, q)));
+    if (h == 0) pdf[q] = p;
+  }
+}
+
+// train.cu:69-172 with the lobes split over a lane pair: each lane computes
+// its lobes' activations, vMF values and gradients; q and the total come
+// from the pair's partial sums.
+template <int K, bool SEL>
+__global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __restrict__ raw, int stride,
+                                                                 const float* __restrict__ rec, int rstride, int n,
+                                                                 float scale, MixOpts o, float* __restrict__ grad,
+                                                                 float* __restrict__ loss,
+                                                                 double* __restrict__ partials) {
+  constexpr int KH = K / 2;
+  constexpr bool FAST = kMixFast;
+  const int h = threadIdx.x & 1;
+  double acc = 0.0;
+  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += long(gridDim.x) * blockDim.x) {
+    const long q = t >> 1;
+    float r[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
+    float swt, cwt, swp, cwp;
+    sincosf(r[0], &swt, &cwt);
+    sincosf(r[1], &swp, &cwp);
+    const f3 wi{swt * cwp, swt * swp, cwt};
+    const float* row = raw + q * stride + h * KH * 4;
+    float lam[KH], kap[KH], dkap[KH], vmf[KH], cc[KH], dta[KH], dpa[KH], sgt[KH], sgp[KH];
+    float lt = 0.f, nt = 0.f;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) {
+      const float4 x = reinterpret_cast<const float4*>(row)[i];
+      lam[i] = xexp<FAST>(act_exp_clamp(x.x));
+      if (o.kappa_softplus) {
+        kap[i] = softplus<FAST>(x.y);
+        dkap[i] = logistic<FAST>(x.y);
+      } else {
+        kap[i] = xexp<FAST>(act_exp_clamp(x.y));
+        dkap[i] = kap[i];  // train.h:410: the derivative ignores the clamp
+      }
+      sgt[i] = logistic<FAST>(x.z);
+      sgp[i] = logistic<FAST>(x.w);
+      float sth, cth, sph, cph;
+      lobe_angles<FAST, true>(sgt[i], sgp[i], &sth, &cth, &sph, &cph);
+      cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
+      dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
+      dpa[i] = (wi.y * cph - wi.x * sph) * sth;
+      const float k = kap[i];
+      vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, cc[i] - 1.f)) * vmf_norm<FAST>(k);
+      lt += lam[i];
+      nt += lam[i] * vmf[i];
+    }
+    const float total = pair_sum(lt);
+    const float qv = pair_sum(nt) / total;
+    const float Li = (r[2] + (r[3] + r[4])) / 3.f;
+    float prefix, l, sel = 1.f;
+    if (SEL) {
+      sel = logistic<FAST>(raw[q * stride + 4 * K]);
+      const float wp = sel * (qv + NMG_EPS) + (1.f - sel) * r[6];
+      l = -Li / wp * logf(wp);
+      prefix = -Li / wp / wp * scale;
+    } else {
+      const float wp = r[5] + NMG_EPS, guide = qv + NMG_EPS;
+      prefix = -Li / wp / guide * scale;
+      l = -Li / wp * logf(guide);
+    }
+    const float inv_total = 1.f / total;
+    float4* gr = reinterpret_cast<float4*>(grad + q * stride) + h * KH;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) {
+      const float k = kap[i];
+      const float wv = (lam[i] * inv_total) * vmf[i];
+      float ik;
+      if (o.kappa_poly && k < 1.f) {
+        ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+      } else if (!o.kappa_poly && k < 1e-2f) {
+        ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+      } else {
+        const float e = xexp<FAST>(-2.f * k);
+        ik = 1.f / k - (1.f + e) / (1.f - e);
+      }
+      float g0 = prefix * ((vmf[i] - qv) * inv_total * sel) * lam[i];
+      float g1 = prefix * (wv * (cc[i] + ik) * sel) * dkap[i];
+      float g2 = prefix * (wv * k * dta[i] * sel) * NMG_PI * (sgt[i] * (1.f - sgt[i]));
+      float g3 = prefix * (wv * k * dpa[i] * sel) * NMG_TWO_PI * (sgp[i] * (1.f - sgp[i]));
+      if (!SEL) {  // train.cu:109-123 (the selection variant has no such pass)
+        g0 = isfinite(g0) ? fminf(g0, 150.f) : 0.f;
+        g1 = isfinite(g1) ? fminf(g1, 150.f) : 0.f;
+        g2 = isfinite(g2) ? fminf(g2, 150.f) : 0.f;
+        g3 = isfinite(g3) ? fminf(g3, 150.f) : 0.f;
+      }
+      gr[i] = make_float4(g0, g1, g2, g3);
+    }
+    if (h == 0) {
+      if (SEL) grad[q * stride + 4 * K] = 0.01f * prefix * (qv - r[6]) * (sel * (1.f - sel));
+      if (loss) loss[q] = l;
+      acc += double(l);
+    }
+  }
+  const double s = block_sum_fixed(acc);
+  if (threadIdx.x == 0 && partials) partials[blockIdx.x] = s;
+}
+
 template <int K>
 static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, const float* u4, const float* cosn,
                                 int n, float* dir, float* pdf, int* lobe, cudaStream_t st) {
+  // one thread per query: splitting the lobes over a lane pair (as the loss does) measured slower here,
+  // the selection and the sampling of the chosen lobe being per-query work both lanes would repeat
   k_mixture_sample<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
                                                                dir, pdf, lobe);
   return check_launch("nmg_mixture_sample");
@@ -133,7 +286,11 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
 template <int K>
 static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const float* wi, const float* cosn, int n,
                              float* pdf, cudaStream_t st) {
-  k_mixture_pdf<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
+  if constexpr (K % 2 == 0)
+    k_mixture_pdf2<K, kMixFast><<<grid_for(2L * n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n,
+                                                                    o->kappa_softplus, pdf);
+  else
+    k_mixture_pdf<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
   return check_launch("nmg_mixture_pdf");
 }
 
@@ -142,14 +299,23 @@ static nmg_status launch_loss(const nmg_mixture_opts* o, const float* raw, const
                               float loss_scale, float* grad, float* loss, double* loss_sum, double* partials,
                               cudaStream_t st) {
   MixOpts mo{o->kappa_softplus, o->kappa_poly, 0};
-  const int blocks = grid_for(n);
+  const int blocks = grid_for(n);  // the workspace holds one partial per block of this grid
   const float scale = loss_scale / float(n);
-  if (o->selection)
-    k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
-                                                              loss_sum ? partials : nullptr);
-  else
-    k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
-                                                               loss_sum ? partials : nullptr);
+  if constexpr (K % 2 == 0) {
+    if (o->selection)
+      k_mixture_loss_grad2<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                 loss, loss_sum ? partials : nullptr);
+    else
+      k_mixture_loss_grad2<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                  loss, loss_sum ? partials : nullptr);
+  } else {
+    if (o->selection)
+      k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                loss, loss_sum ? partials : nullptr);
+    else
+      k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                 loss, loss_sum ? partials : nullptr);
+  }
   nmg_status s = check_launch("nmg_mixture_loss_grad");
   if (s != NMG_OK || !loss_sum) return s;
   k_sum_partials<<<1, 256, 0, st>>>(partials, blocks, loss_sum);
@@ -314,12 +480,22 @@ static nmg_status launch_loss_noalloc(const nmg_mixture_opts* o, const float* ra
   MixOpts mo{o->kappa_softplus, o->kappa_poly, 0};
   const int blocks = (n + kThreads - 1) / kThreads;  // one partial per block, every slot rewritten
   const float scale = loss_scale / float(n);
-  if (o->selection)
-    k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
-                                                              loss_sum ? partials : nullptr);
-  else
-    k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad, loss,
-                                                               loss_sum ? partials : nullptr);
+  // the kernels of nmg_mixture_loss_grad, so that both entry points give the same gradients
+  if constexpr (K % 2 == 0) {
+    if (o->selection)
+      k_mixture_loss_grad2<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                 loss, loss_sum ? partials : nullptr);
+    else
+      k_mixture_loss_grad2<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                  loss, loss_sum ? partials : nullptr);
+  } else {
+    if (o->selection)
+      k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                loss, loss_sum ? partials : nullptr);
+    else
+      k_mixture_loss_grad<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                 loss, loss_sum ? partials : nullptr);
+  }
   nmg_status s = check_launch("nmg_mixture_loss_grad_noalloc");
   if (s != NMG_OK || !loss_sum) return s;
   k_sum_partials<<<1, 256, 0, st>>>(partials, blocks, loss_sum);
