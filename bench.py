@@ -115,13 +115,20 @@ def dist_setup():
 
 
 def barrier_max(x, ws):
+    """Maximum of x over the ranks (the job's time is its slowest replica's)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], device="cuda", dtype=torch.float64)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], device=dev, dtype=torch.float64)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seed(rank, base=7272):
+    """Each replica draws its own synthetic wavefront and training batch."""
+    return base + rank
 
 
 def make_inputs(synth, torch, seed=7272):
@@ -139,7 +146,7 @@ def run_ours(args):
     synth = importlib.import_module(PKG + ".synth")
     ws, rank = dist_setup()
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    q, x, rec = make_inputs(synth, torch, seed=7272 + rank)
+    q, x, rec = make_inputs(synth, torch, seed=replica_seed(rank))
     dq = {k: torch.from_numpy(np.ascontiguousarray(v)).cuda() for k, v in q.items()}
     dx, drec = torch.from_numpy(x).cuda(), torch.from_numpy(rec).cuda()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
