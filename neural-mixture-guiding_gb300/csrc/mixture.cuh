@@ -89,14 +89,13 @@ NMG_D void lobe_angles(float st, float sp, float* sth, float* cth, float* sph, f
 
 // -expm1(-x) = 1 - e^{-x} for x >= 0 without cancellation: a degree-7 Taylor
 // polynomial below x = 0.5 (relative error < 3e-8), 1 - e^{-x} above.
-// Both branches are evaluated and one is selected: lanes of a warp rarely
-// agree on the side of 0.5, and a branch would run both anyway.
+// (A branch-free select of both forms measured slower in the fused query
+// kernel: the extra live values made its consumer warps spill.)
 template <bool FAST> NMG_D float one_minus_exp_neg(float x) {
   if (!FAST) return -expm1f(-x);
-  const float big = 1.f - __expf(-x);
-  const float small = x * (1.f - x * (1.f / 2.f) * (1.f - x * (1.f / 3.f) * (1.f - x * (1.f / 4.f) *
-                      (1.f - x * (1.f / 5.f) * (1.f - x * (1.f / 6.f) * (1.f - x * (1.f / 7.f)))))));
-  return x >= 0.5f ? big : small;
+  if (x >= 0.5f) return 1.f - __expf(-x);
+  return x * (1.f - x * (1.f / 2.f) * (1.f - x * (1.f / 3.f) * (1.f - x * (1.f / 4.f) *
+             (1.f - x * (1.f / 5.f) * (1.f - x * (1.f / 6.f) * (1.f - x * (1.f / 7.f)))))));
 }
 template <bool FAST> NMG_D f3 unit3(f3 a) {
   if (!FAST) return normalize3(a);

@@ -314,6 +314,8 @@ __global__ void __launch_bounds__(256) k_adam_ema(AdamArgs a, const float4* __re
   const float debias_old = 1.f - exp2f(float(step - 1) * a.log2_decay);
   const float debias_new = 1.f / (1.f - exp2f(float(step) * a.log2_decay));
   const bool separate_inf = w_inf != w;
+  // squared-gradient sum: FP32 within each group of four (the FP64 pipe of
+  // this GPU is narrow), FP64 across groups and threads
   double gn = 0.0;
   for (long j = long(blockIdx.x) * blockDim.x + threadIdx.x; j < a.n4; j += long(gridDim.x) * blockDim.x) {
     const bool matrix = 4 * j < a.n_matrix;
@@ -322,11 +324,13 @@ __global__ void __launch_bounds__(256) k_adam_ema(AdamArgs a, const float4* __re
     float4 w4 = w[j];
     float ww[4] = {w4.x, w4.y, w4.z, w4.w};
     bool any = matrix;
+    float g2 = 0.f;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      gn += double(gg[k]) * double(gg[k]);
+      g2 = fmaf(gg[k], gg[k], g2);
       any |= gg[k] != 0.f;
     }
+    gn += double(g2);
     if (any) {
       float4 m4 = m[j], v4 = v[j];
       uint4 t4 = psteps[j];
