@@ -177,7 +177,10 @@ NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* ou
 
 // Encodes one input row x into `tile` row `row` (KC 16-byte chunks).
 // UNROLL = false keeps one copy of the chunk body (smaller code for kernels
-// whose instruction footprint matters more than the loop overhead).
+// whose instruction footprint matters more than the loop overhead). Levels
+// are gathered one at a time: computing the corners of 2 or 4 levels first
+// and issuing all their table loads back to back measured slower in both
+// fused kernels.
 template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH, bool UNROLL = true>
 NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, int row) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;

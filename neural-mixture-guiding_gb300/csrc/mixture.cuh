@@ -52,9 +52,11 @@ template <bool FAST> NMG_D void xsincos_turn(float t, float* s, float* c) {
 // (t - 1, 1 - t and 0.5 - t are exact where they are taken) onto [0, 1/4],
 // where Taylor polynomials of degree 9 (sin) and 8 (cos) of x = pi t are
 // accurate to 2e-9 and 3e-8; over [0, 2] the result is within 1e-7 of the
-// exact value (tested against double precision on 2e7 points).
+// exact value (tested against double precision on 2e7 points). TWO = false
+// drops the fold of [1, 2] onto [0, 1] for arguments known to lie in [0, 1].
+template <bool TWO = true>
 NMG_HD void sincospi_poly(float t, float* s, float* c) {
-  const bool hi = t >= 1.f;
+  const bool hi = TWO && t >= 1.f;
   const float t1 = hi ? t - 1.f : t;
   const bool upper = t1 > 0.5f;
   const float a = upper ? 1.f - t1 : t1;
@@ -76,11 +78,13 @@ NMG_HD void sincospi_poly(float t, float* s, float* c) {
 // ~1e-7; the hardware approximation (FAST and not PRECISE) is off by up to
 // ~4e-7, which a lobe of concentration kappa turns into a relative pdf
 // error of ~4e-7 kappa.
-template <bool FAST, bool PRECISE>
+// FOLD01 = false keeps the general fold for theta as well (shorter code is
+// not always faster: it changes the register allocation of the caller).
+template <bool FAST, bool PRECISE, bool FOLD01 = true>
 NMG_D void lobe_angles(float st, float sp, float* sth, float* cth, float* sph, float* cph) {
   if (PRECISE) {
-    sincospi_poly(st, sth, cth);
-    sincospi_poly(2.f * sp, sph, cph);
+    sincospi_poly<!FOLD01>(st, sth, cth);
+    sincospi_poly<true>(2.f * sp, sph, cph);
   } else {
     xsincos<FAST>(NMG_PI * st, sth, cth);
     xsincos_turn<FAST>(sp, sph, cph);
@@ -153,9 +157,10 @@ NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
     m.mu[i] = f3{st * cp, st * sp, ct};
     m.total += m.lam[i];
   }
+  const float inv = 1.f / m.total;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    m.w[i] = m.lam[i] / m.total;
+    m.w[i] = FAST ? m.lam[i] * inv : m.lam[i] / m.total;
     m.nrm[i] = vmf_norm<FAST>(m.kap[i]);
   }
 }
@@ -359,7 +364,7 @@ NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, cons
     }
     sgt[i] = logistic<FAST>(r.z);
     sgp[i] = logistic<FAST>(r.w);
-    lobe_angles<FAST, PRECISE>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
+    lobe_angles<FAST, PRECISE, false>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
     total += lam[i];
   }
   float swt, cwt, swp, cwp;
@@ -436,7 +441,7 @@ NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float s
     }
     sgt[i] = logistic<FAST>(r.z);
     sgp[i] = logistic<FAST>(r.w);
-    lobe_angles<FAST, PRECISE>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
+    lobe_angles<FAST, PRECISE, false>(sgt[i], sgp[i], &sth[i], &cth[i], &sph[i], &cph[i]);
     total += lam[i];
   }
   const float xs = raw_at(raw, 4 * K);

@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       sgt[i] = logistic<FAST>(x.z);
       sgp[i] = logistic<FAST>(x.w);
       float sth, cth, sph, cph;
-      lobe_angles<FAST, true>(sgt[i], sgp[i], &sth, &cth, &sph, &cph);
+      lobe_angles<FAST, true, false>(sgt[i], sgp[i], &sth, &cth, &sph, &cph);
       cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
       dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
       dpa[i] = (wi.y * cph - wi.x * sph) * sth;
