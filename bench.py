@@ -41,6 +41,10 @@ BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, roug
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query_ws launch over the same
 # 2,073,600-query wavefront (ncu capture summarised in profiles/k_fused_query_ws_hashgrid_2073600.md)
 TRAFFIC_QUERY_BYTES = 141_327_616 + 37_800_704
+# l1tex__m_xbar2l1tex_read_bytes.sum of the same capture: the hash-grid corner gathers reaching L2
+# (the 24 MB table stays in L2), in 32-byte sectors; about one sector request per cycle per SM is
+# the ceiling a gather-only kernel of the same 128 corners per query reaches
+L2_TO_L1_BYTES = 4.80e9
 
 
 def peaks():
@@ -303,9 +307,10 @@ def run_ours(args):
                      "frac": tflops / bf16, "peak_source": src,
                      "traffic": TRAFFIC_QUERY_BYTES if path == nmg.PATH_BF16 else None,
                      "traffic_unit": "bytes per launch (ncu)",
-                     "limiter": "hash-grid gathers: ~69 L2 sector requests per query, L1->L2 request path 71% busy "
+                     "limiter": "hash-grid gathers: ~72 L2 sector requests per query, L1->L2 request path 71% busy "
                                 "(ncu), not HBM or the tensor pipe",
                      "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm,
+                     "l2_sector_requests": l2_request_roofline(t_kernel, ours["clocks"]),
                      "per_unit": {"flop_per_query": FLOP_PER_QUERY, "hbm_bytes_per_query": BYTES_PER_QUERY},
                      "kernel_ms": t_kernel * 1e3},
         "cpu_baseline": cpu,
@@ -368,6 +373,17 @@ def frame_graph(nmg, synth, torch, np, dx, drec, path, lobes=(8, 16), frames=5, 
         fr.close()
         f.close()
     return res
+
+
+def l2_request_roofline(t_kernel, clocks, sms=152):
+    """The query kernel's real limiter: L2 -> L1 sector requests per SM and cycle (ncu byte count of
+    one launch / 32 B, over the CUDA-event kernel time at the SM clock sampled in the timed region)
+    against the ~1 request / cycle / SM ceiling of a gather-only kernel."""
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    sectors = L2_TO_L1_BYTES / 32
+    per_sm_clk = sectors / (t_kernel * sms * mhz * 1e6)
+    return {"sectors_per_query": sectors / N_QUERIES, "achieved_per_sm_per_clk": per_sm_clk,
+            "ceiling_per_sm_per_clk": 1.0, "frac": per_sm_clk, "source": "ncu byte count, live kernel time"}
 
 
 class L2Flush:
