@@ -301,7 +301,7 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
 /*
  * nmg_query and nmg_train_step on HOST buffers (pinned memory gives the
  * overlap; pageable memory works but copies synchronously). nmg_query_host
- * splits the wavefront into up to 8 chunks of at least 2^18 queries and
+ * splits the wavefront into up to 4 chunks of at least 2^18 queries and
  * pipelines them over three streams: inputs of chunk i+1 go to the device
  * while chunk i is computed on `stream` and the outputs of chunk i-1 come
  * back. Every input and output array (all of in, u4, out->dir, out->pdf and,

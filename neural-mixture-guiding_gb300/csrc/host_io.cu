@@ -26,9 +26,13 @@
 namespace nmg {
 
 // The first chunk's inputs and the last chunk's outputs cannot overlap a
-// kernel, so more, smaller chunks shorten that exposed copy time; below about
-// 2^18 queries a chunk leaves the persistent grid underfilled.
-constexpr int kMaxChunks = 8;
+// kernel, so more, smaller chunks shorten that exposed copy time, but every
+// chunk is one more launch of the persistent query kernel, whose pipeline
+// fill and last-round imbalance cost ~19 us per launch: a 1920x1080 query
+// pass plus training step on host buffers measured 1.39 ms with 4 chunks,
+// 1.41 with 2, 1.42 with 7 and 1.58 with 15. Below about 2^18 queries a
+// chunk leaves the persistent grid underfilled.
+constexpr int kMaxChunks = 4;
 constexpr int kMinChunk = 1 << 18;
 
 struct HostIO {
