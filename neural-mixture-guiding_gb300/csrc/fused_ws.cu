@@ -1,7 +1,7 @@
 // fused_ws.cu -- warp-specialised fused query kernel.
 //
 // The query pass spends most of its time on the hash-grid corner gathers: 128
-// four-byte loads per query into the L2-resident table, which reach L1 as ~69
+// four-byte loads per query into the L2-resident table, which reach L1 as ~70
 // separate 32-byte sector requests. An SM issues about one such request per
 // cycle, and it only does so while enough of its threads are gathering. In
 // the one-kernel-per-warpgroup design (fused.cu) every warpgroup alternates
