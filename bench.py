@@ -401,8 +401,8 @@ class L2Flush:
 
 
 def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
-    """The mixture-only workload (K = 8 raw outputs per query, no network) at the size SURVEY-style
-    bandwidth figures use, 2^21 queries: sample+pdf and KL loss+gradient, CUDA events, L2 flushed.
+    """The mixture-only workload (K = 8 raw outputs per query, no network) at a size whose traffic
+    dwarfs L2, 2^21 queries: sample+pdf and KL loss+gradient, CUDA events, L2 flushed.
     Algorithmic bytes per query: 164 (raw 128 + uniforms 16 in; direction 12, pdf 4, lobe 4 out) and
     284 (raw 128 + record 28 in; gradient 128 out)."""
     raw, u4, rec = synth.mixture_batch(n, K, seed=7272, selection=False)
