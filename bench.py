@@ -40,11 +40,11 @@ FLOP_PER_QUERY = 2 * (80 * 64 + 64 * 64 + 64 * 64 + 64 * 48)  # 32,768 executed 
 BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, rough, u4 in; dir, pdf, lobe, sel out
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query_ws launch over the same
 # 2,073,600-query wavefront (ncu capture summarised in profiles/k_fused_query_ws_hashgrid_2073600.md)
-TRAFFIC_QUERY_BYTES = 141_316_608 + 36_785_152
+TRAFFIC_QUERY_BYTES = 141_388_032 + 37_773_312
 # l1tex__m_xbar2l1tex_read_bytes.sum of the same capture: the hash-grid corner gathers reaching L2
 # (the 24 MB table stays in L2), in 32-byte sectors; about one sector request per cycle per SM is
 # the ceiling a gather-only kernel of the same 128 corners per query reaches
-L2_TO_L1_BYTES = 4.640e9
+L2_TO_L1_BYTES = 4.679e9
 
 
 def peaks():
@@ -307,7 +307,7 @@ def run_ours(args):
                      "frac": tflops / bf16, "peak_source": src,
                      "traffic": TRAFFIC_QUERY_BYTES if path == nmg.PATH_BF16 else None,
                      "traffic_unit": "bytes per launch (ncu)",
-                     "limiter": "hash-grid gathers: ~70 L2 sector requests per query, L1->L2 request path 70% busy "
+                     "limiter": "hash-grid gathers: ~70 L2 sector requests per query, L1->L2 request path 74% busy "
                                 "(ncu), not HBM or the tensor pipe",
                      "hbm_achieved_gbs": gbs, "hbm_frac": gbs / hbm,
                      "l2_sector_requests": l2_request_roofline(t_kernel, ours["clocks"]),

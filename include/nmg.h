@@ -341,7 +341,8 @@ nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int 
  * warpgroups feed MLP + mixture warpgroups through a shared-memory ring
  * (8: 4 + 2 warpgroups, 4 slots; 9: 5 + 1, 5 slots; 10: 6 + 2, 6 slots;
  * 11: 4 + 2, 8 slots; 12: 4 + 2, 4 slots holding the hidden activations too).
- * 0 selects the default: 8, or 4 for 16-lobe networks. nmg_get_query_tiling
+ * 0 selects the default: 12 for the 8-lobe hash-grid network, 8 for the
+ * reference network, 4 for 16-lobe networks. nmg_get_query_tiling
  * reports the tiling in use (0 on the FP32 path). No counterpart in the
  * reference (its FullyFusedMLP launch shape is fixed,
  * fully_fused_mlp.cu:500-558).

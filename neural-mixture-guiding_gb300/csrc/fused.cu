@@ -225,12 +225,15 @@ static nmg_status launch_query(const FusedArgs& a, int nwg, cudaStream_t st) {
 
 // Default query tiling: the warp-specialised kernel (4 encoder + 2 consumer
 // warpgroups) for the 8-lobe networks, measured 1.3x faster than one
-// pipeline per warpgroup on a 2,073,600-query wavefront; the 16-lobe
-// network's consumer epilogue does not fit 128 registers, so it keeps the
-// one-pipeline-per-warpgroup kernel.
+// pipeline per warpgroup on a 2,073,600-query wavefront; for the hash-grid
+// network its variant with the hidden activations kept in the ring slot
+// (tiling 12: 32 KB more L1 for the table gathers) measured 630 us against
+// 646 us. The 16-lobe network's consumer epilogue does not fit 128
+// registers, so it keeps the one-pipeline-per-warpgroup kernel.
 int fused_default_tiling(const nmg_ctx* c) {
   const FusedState* s = reinterpret_cast<const FusedState*>(c->ws.fused);
-  return s && s->preset != 2 ? kTilingWarpSpecialised : 4;
+  if (!s || s->preset == 2) return 4;
+  return s->preset == 1 ? kTilingWarpSpecialised + 4 : kTilingWarpSpecialised;
 }
 
 static nmg_status dispatch_query(nmg_ctx* c, const FusedArgs& a, cudaStream_t st) {

@@ -121,8 +121,14 @@ NMG_D void load_feats(const uint16_t* table, uint32_t entry, float* v, bool fp16
 // weights follow grid.h:221-385; the corner indices are formed from per-axis
 // terms (x, y*P1, z*P2 for hashed levels, x, y*res, z*res^2 for dense ones),
 // which equal grid_index's value for every corner, and the corner weight is
-// (w_x' * w_y') * w_z' as in the reference.
-template <int F, bool SMOOTH>
+// (w_x' * w_y') * w_z' as in the reference. PAIR (F = 2): the x and x+1
+// corners of a (y, z) pair that share an aligned 8-byte word (every other
+// cell: for dense levels e1 = e0 + 1, for hashed ones e1 = e0 ^ 1 when x is
+// even) are read with one 8-byte load -- a quarter fewer L1 requests in
+// the query kernel's encoders (648 instead of 678 us); the training kernel,
+// whose compute warpgroups gather with more registers, measured 1% slower
+// with it.
+template <int F, bool SMOOTH, bool PAIR = false>
 NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* out) {
   float w[3];
   uint32_t g[3];
@@ -163,13 +169,37 @@ NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* ou
   float acc[F];
 #pragma unroll
   for (int k = 0; k < F; ++k) acc[k] = 0.f;
+  if constexpr (PAIR && F == 2) {
+    const bool fp16 = a.fp16 != 0;
+    const uint32_t* tw = reinterpret_cast<const uint32_t*>(a.table);
 #pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    const float wt = wxy[c & 3] * wz[c >> 2];
-    float v[F];
-    load_feats<F>(a.table, e[c], v, a.fp16 != 0);
+    for (int c = 0; c < 8; c += 2) {
+      uint32_t w0, w1;
+      if ((e[c] ^ e[c + 1]) == 1u) {  // entries 2m and 2m+1
+        const uint2 w = __ldg(reinterpret_cast<const uint2*>(tw + (e[c] & ~1u)));
+        const bool lo0 = e[c] < e[c + 1];
+        w0 = lo0 ? w.x : w.y;
+        w1 = lo0 ? w.y : w.x;
+      } else {
+        w0 = __ldg(tw + e[c]);
+        w1 = __ldg(tw + e[c + 1]);
+      }
+      const float2 v0 = tc::unpack2(w0, fp16), v1 = tc::unpack2(w1, fp16);
+      const float wt0 = wxy[c & 3] * wz[c >> 2], wt1 = wxy[(c + 1) & 3] * wz[c >> 2];
+      acc[0] = fmaf(wt0, v0.x, acc[0]);  // same corner order as below
+      acc[1] = fmaf(wt0, v0.y, acc[1]);
+      acc[0] = fmaf(wt1, v1.x, acc[0]);
+      acc[1] = fmaf(wt1, v1.y, acc[1]);
+    }
+  } else {
 #pragma unroll
-    for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
+    for (int c = 0; c < 8; ++c) {
+      const float wt = wxy[c & 3] * wz[c >> 2];
+      float v[F];
+      load_feats<F>(a.table, e[c], v, a.fp16 != 0);
+#pragma unroll
+      for (int k = 0; k < F; ++k) acc[k] = fmaf(wt, v[k], acc[k]);
+    }
   }
 #pragma unroll
   for (int k = 0; k < F; ++k) out[k] = acc[k];
@@ -181,7 +211,7 @@ NMG_D void grid_level(const FusedArgs& a, int l, const float (&p3)[3], float* ou
 // are gathered one at a time: computing the corners of 2 or 4 levels first
 // and issuing all their table loads back to back measured slower in both
 // fused kernels.
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH, bool UNROLL = true>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH, bool UNROLL = true, bool PAIR = false>
 NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, int row) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NGRID = LEVELS * F;
@@ -195,7 +225,7 @@ NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, i
   for (int ch = 0; ch < NGRID / 8; ++ch) {
     float f[8];
 #pragma unroll
-    for (int j = 0; j < LPC; ++j) grid_level<F, SMOOTH>(a, ch * LPC + j, p3, f + j * F);
+    for (int j = 0; j < LPC; ++j) grid_level<F, SMOOTH, PAIR>(a, ch * LPC + j, p3, f + j * F);
     store_chunk(tile, row, ch, KC, f, fp16);
   }
   float d[NPAD - NGRID];

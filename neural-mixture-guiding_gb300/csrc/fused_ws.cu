@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
         else
           featurize<true>(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
       }
-      encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, false>(a, x, slots + s * SLOT, t);
+      encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, false, true>(a, x, slots + s * SLOT, t);
       tc::fence_proxy_async();
       tc::mbar_arrive(&full[s]);
     }
