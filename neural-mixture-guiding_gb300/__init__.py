@@ -396,6 +396,9 @@ class GuidingField:
             b.train_count = cnt.data_ptr() if cnt is not None else None
             b.train_n_max = int(x.shape[0])
             b.stats = st.data_ptr() if st is not None else None
+        # the structure holds raw device pointers: keep the tensors (the count in particular,
+        # which callers often create inline) alive for as long as the bounce is
+        b._keep = (pos, wo, normal, rough, u4, dict(outputs), count, train)
         return b
 
     def capture_frame(self, bounces):
@@ -403,7 +406,8 @@ class GuidingField:
         arr = (Bounce * len(bounces))(*bounces)
         h = C.c_void_p()
         check(self.L.nmg_frame_capture(self.h, arr, len(bounces), C.byref(h)))
-        return Frame(self.L, h, arr)
+        # the graph replays with the bounces' device pointers: the frame keeps their tensors alive
+        return Frame(self.L, h, (arr, [getattr(b, "_keep", None) for b in bounces]))
 
     def run_frame_eager(self, bounces, stream=None):
         arr = (Bounce * len(bounces))(*bounces)

@@ -84,3 +84,33 @@ def test_frame_graph_matches_eager_and_follows_device_counts(nmg, synth, K):
     frame.close()
     a.close()
     b.close()
+
+
+def test_frame_keeps_inline_count_tensors_alive(nmg, synth):
+    """A count tensor created inline in GuidingField.bounce (no other reference) must stay valid
+    for the captured graph: the binding keeps every tensor of a bounce alive with the frame."""
+    import gc
+
+    import torch
+    qs, x, rec = _inputs(synth, torch)
+    f = nmg.GuidingField(nmg.config(1, path=nmg.PATH_BF16), max_queries=SIZES[0], max_batch=BATCH)
+    outs, bounces = [], []
+    for q in qs[:3]:
+        n = q["pos"].shape[0]
+        o = {"dir": torch.empty((n, 3), device="cuda"), "pdf": torch.full((n,), float("nan"), device="cuda"),
+             "lobe": torch.empty(n, device="cuda", dtype=torch.int32), "selection": torch.empty(n, device="cuda")}
+        outs.append(o)
+        bounces.append(nmg.GuidingField.bounce(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"], o,
+                                               count=torch.tensor([n], device="cuda", dtype=torch.int32),
+                                               train=(x, rec, None, None)))
+    frame = f.capture_frame(bounces)
+    del bounces
+    gc.collect()
+    # small allocations that would take over freed count storage, overwritten with zeros
+    scratch = [torch.zeros(1, device="cuda", dtype=torch.int32) for _ in range(64)]
+    frame.launch()
+    torch.cuda.synchronize()
+    for o in outs:
+        assert bool(torch.isfinite(o["pdf"]).all()) and bool((o["pdf"] > 0).all())
+    del scratch
+    frame.close()
