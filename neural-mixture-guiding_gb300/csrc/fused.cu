@@ -34,7 +34,11 @@
 
 namespace nmg {
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
+// STREAM: the mixture epilogue reads the raw outputs from TMEM lobe group by
+// lobe group (query_epilogue_streamed) instead of holding them in registers;
+// used for 16-lobe queries that return no raw outputs.
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG,
+          bool STREAM = false>
 __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_constant__ FusedArgs a) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
@@ -82,6 +86,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
   const int ntiles = (n + kRows - 1) / kRows;
   const int nl = a.n_layers;
   const uint32_t a_addr = tc::smem_u32(A);
+  constexpr bool streamed = STREAM;
 
   // Every early exit below follows a warpgroup-wide bar.red.and, so the 128
   // threads of a group always leave the loop together (no thread can be
@@ -136,18 +141,26 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
         ok = bar_red_and(1 + wg, kRows, done);
         if (!ok) break;
       } else {
+        if constexpr (!streamed) {
 #pragma unroll
-        for (int c = 0; c < NOUTMAX / 16; ++c)
-          if (c * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + c * 16, r + 16 * c);
-        tc::tmem_wait_ld();
+          for (int c = 0; c < NOUTMAX / 16; ++c)
+            if (c * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + c * 16, r + 16 * c);
+          tc::tmem_wait_ld();
+        }
         last_ok = done;
       }
     }
     if (!ok) break;
-    ok = last_ok;  // reconciled across the group at the next tile's barrier
     // ---- epilogue: raw outputs and/or mixture
-    if (valid && ok) {
-      query_epilogue<K, NOUTMAX>(a, q, r);
+    if constexpr (streamed) {
+      // warp-collective TMEM reads: the group agrees on ok first; the accumulator stays
+      // untouched until the next tile's layer 0, issued after the group's next barrier
+      ok = bar_red_and(1 + wg, kRows, last_ok);
+      if (!ok) break;
+      query_epilogue_streamed<K>(a, q, valid, lane_addr);
+    } else {
+      ok = last_ok;  // reconciled across the group at the next tile's barrier
+      if (valid && ok) query_epilogue<K, NOUTMAX>(a, q, r);
     }
   }
   if (!ok && t == 0) atomicExch(a.err, 2);
@@ -199,6 +212,8 @@ static size_t smem_bytes_for(uint32_t w_bytes) {
 template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG>
 static nmg_status launch_query_nwg(const FusedArgs& a, cudaStream_t st) {
   auto kern = k_fused_query<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG>;
+  if constexpr (K == 16)
+    if (!a.raw && !a.raw_mode) kern = k_fused_query<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, true>;
   const size_t smem = smem_bytes_for<F, LEVELS, MODE, SHDEG, BINS, NWG>(a.w_bytes);
   nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
   if (s != NMG_OK) return s;

@@ -280,6 +280,124 @@ NMG_D void query_epilogue(const FusedArgs& a, long q, const float (&r)[NOUTMAX])
   if (a.sel && a.selection) a.sel[q] = logistic<true>(r[4 * K < NOUTMAX ? 4 * K : 0]);
 }
 
+// query_epilogue for wide mixtures (K = 16) with the raw outputs left in
+// TMEM: holding all K lobes (7 K floats) next to the 4 K raw outputs does not
+// fit the registers of a 128-query warpgroup, so this variant keeps only the
+// K lobe weights and derives each lobe again from its 4 raw outputs
+// (tcgen05.ld of 16 columns = 4 lobes) when it is needed: once for the
+// weights, once for the sampled lobe, once for the pdf. The lobe arithmetic
+// is that of query_epilogue (same helpers, same order), so the results are
+// the same. Warp-collective: every thread of the warpgroup calls it with its
+// TMEM row address; rows past n (valid = false) compute and store nothing.
+template <int K>
+NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint32_t lane_addr) {
+  static_assert(K % 4 == 0, "lobes come in groups of four (16 TMEM columns)");
+  constexpr int G = K / 4;
+  const bool cosine = a.mix.cosine != 0;
+  f3 mb{0.f, 0.f, 1.f};
+  if (cosine && valid) mb = unit3<true>(face_fwd(load3(a.nrm, q), load3(a.wo, q)));
+  const float nb = prod_norm<true>(kCosineKappa);
+  // lobe i of the 16-column group in v, as query_epilogue's activation (+ cosine product) makes it
+  auto lobe = [&](const float (&v)[16], int j, float& lam, float& kap, f3& mu, float& nrm) {
+    lobe_activate<true>(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3], a.mix.kappa_softplus, lam, kap, mu);
+    nrm = vmf_norm<true>(kap);
+    if (cosine) lobe_cosine<true>(mb, nb, lam, kap, mu, nrm);
+  };
+  // pass 1: weights
+  float lw[K];
+  float total = 0.f;
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    float v[16];
+    tc::tmem_ld16(lane_addr + 16 * g, v);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float lam, kap, nrm;
+      f3 mu;
+      lobe(v, j, lam, kap, mu, nrm);
+      lw[4 * g + j] = lam;
+      total += lam;
+    }
+  }
+  if (cosine) total = fmaxf(total, NMG_EPS);  // distribution.h:191
+  const float inv = 1.f / total;
+#pragma unroll
+  for (int i = 0; i < K; ++i) lw[i] *= inv;
+  f3 d;
+  int sel = 0;
+  if (a.wi) {
+    d = valid ? load3(a.wi, q) : f3{0.f, 0.f, 1.f};
+  } else {
+    // selection (distribution.h:132-140) and pass 2: the selected lobe, sampled
+    const float4 u = valid ? reinterpret_cast<const float4*>(a.u4)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+    float uu = u.y;
+    sel = -1;
+#pragma unroll
+    for (int i = 0; i < K; ++i) {
+      if (sel < 0) {
+        if (uu < lw[i])
+          sel = i;
+        else
+          uu -= lw[i];
+      }
+    }
+    sel = sel < 0 ? 0 : sel;
+    float ks = 0.f;
+    f3 ms{0.f, 0.f, 1.f};
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      float v[16];
+      tc::tmem_ld16(lane_addr + 16 * g, v);
+      tc::tmem_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float lam, kap, nrm;
+        f3 mu;
+        lobe(v, j, lam, kap, mu, nrm);
+        if (4 * g + j == sel) {
+          ks = kap;
+          ms = mu;
+        }
+      }
+    }
+    d = vmf_sample_dir<true>(ks, ms, u.z, u.w);
+  }
+  // pass 3: pdf at d (distribution.h:113-119)
+  float p = 0.f;
+#pragma unroll
+  for (int g = 0; g < G; ++g) {
+    float v[16];
+    tc::tmem_ld16(lane_addr + 16 * g, v);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      float lam, kap, nrm;
+      f3 mu;
+      lobe(v, j, lam, kap, mu, nrm);
+      const float c = dot3(d, mu);
+      const float vv = kap < NMG_EPS ? NMG_INV_4PI : __expf(kap * fminf(0.f, c - 1.f)) * nrm;
+      p += lw[4 * g + j] * vv;
+    }
+  }
+  float slogit = 0.f;
+  if (a.sel && a.selection) {  // the selection logit follows the lobes (column 4K)
+    float v[16];
+    tc::tmem_ld16(lane_addr + 4 * K, v);
+    tc::tmem_wait_ld();
+    slogit = v[0];
+  }
+  if (!valid) return;
+  if (a.wi) {
+    a.pdf[q] = p;
+    return;
+  }
+  store3(a.dir, q, d);
+  a.pdf[q] = p;
+  if (a.lobe) a.lobe[q] = sel;
+  if (a.sel && a.selection) a.sel[q] = logistic<true>(slogit);
+}
+
 // ------------------------------------------------------------ weight image
 struct PackArgs {
   long off[kMaxLayers + 1];

@@ -166,6 +166,17 @@ NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
   }
 }
 
+// One lobe of mix_activate_regs from its raw (lambda, kappa, theta, phi).
+template <bool FAST>
+NMG_D void lobe_activate(float r0, float r1, float r2, float r3, int kappa_softplus, float& lam, float& kap,
+                         f3& mu) {
+  lam = xexp<FAST>(act_exp_clamp(r0));
+  kap = kappa_softplus ? softplus<FAST>(r1) : xexp<FAST>(act_exp_clamp(r1));
+  float st, ct, sp, cp;
+  lobe_angles<FAST, !FAST>(logistic<FAST>(r2), logistic<FAST>(r3), &st, &ct, &sp, &cp);
+  mu = f3{st * cp, st * sp, ct};
+}
+
 // Same activation from raw outputs held in registers (compile-time indices).
 template <int K, bool FAST, int N>
 NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplus) {
@@ -173,11 +184,8 @@ NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplu
   m.total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    m.lam[i] = xexp<FAST>(act_exp_clamp(raw[4 * i]));
-    m.kap[i] = kappa_softplus ? softplus<FAST>(raw[4 * i + 1]) : xexp<FAST>(act_exp_clamp(raw[4 * i + 1]));
-    float st, ct, sp, cp;
-    lobe_angles<FAST, !FAST>(logistic<FAST>(raw[4 * i + 2]), logistic<FAST>(raw[4 * i + 3]), &st, &ct, &sp, &cp);
-    m.mu[i] = f3{st * cp, st * sp, ct};
+    lobe_activate<FAST>(raw[4 * i], raw[4 * i + 1], raw[4 * i + 2], raw[4 * i + 3], kappa_softplus, m.lam[i],
+                        m.kap[i], m.mu[i]);
     m.total += m.lam[i];
   }
   const float inv = 1.f / m.total;
@@ -188,53 +196,64 @@ NMG_D void mix_activate_regs(Mix<K>& m, const float (&raw)[N], int kappa_softplu
   }
 }
 
+// Product normaliser k / (2 pi (1 - e^{-2k})) (distribution.h:40-42): 1/4pi
+// below kappa = 1e-3.
+template <bool FAST> NMG_D float prod_norm(float k) {
+  return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, one_minus_exp_neg<FAST>(2.f * k));
+}
+constexpr float kCosineKappa = 2.18853f;  // distribution.h:184-195
+
+// One lobe (lam, kap, mu, nrm = its vMF normaliser) times the cosine lobe of
+// concentration kb = kCosineKappa around the unit mean mb (nb = its product
+// normaliser): the lobe's new weight, concentration, mean and normaliser.
+template <bool FAST>
+NMG_D void lobe_cosine(f3 mb, float nb, float& lam, float& kap, f3& mu, float& nrm) {
+  const float kb = kCosineKappa;
+  const f3 ma = mu;
+  const float ka = kap;
+  f3 nm = add3(scale3(ma, ka), scale3(mb, kb));
+  const float n2 = dot3(nm, nm);
+  float nk;
+  if (FAST) {
+    const float rn = rsqrtf(n2);
+    nk = n2 * rn;
+    if (nk >= 1e-3f) {
+      nm = scale3(nm, rn);
+    } else {
+      nk = 0.f;
+      nm = ma;
+    }
+  } else {
+    nk = sqrtf(n2);
+    if (nk >= 1e-3f) {
+      nm = f3{nm.x / nk, nm.y / nk, nm.z / nk};
+    } else {
+      nk = 0.f;
+      nm = ma;
+    }
+  }
+  const float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
+  const float pk = prod_norm<FAST>(nk);
+  // prod_norm(ka) equals the lobe's cached vMF normaliser above kappa = 1e-3
+  const float pa = FAST ? (ka < 1e-3f ? NMG_INV_4PI : nrm) : prod_norm<FAST>(ka);
+  const float sc = xdiv<FAST>(pa * nb, pk) * e;
+  lam = sc * lam;
+  kap = nk;
+  mu = nm;
+  nrm = pk;  // equals vmf_norm(nk): nk is 0 or >= 1e-3 here
+}
+
 // distribution.h:39-64 + 184-195: product of every lobe with the cosine lobe
 // (kappa 2.18853) around `n` (already face-forwarded, any length), then
 // renormalisation with total clamped below at M_EPSILON.
 template <int K, bool FAST>
 NMG_D void mix_apply_cosine(Mix<K>& m, f3 n) {
-  const float kb = 2.18853f;
   const f3 mb = unit3<FAST>(n);
-  // product normaliser (distribution.h:40-42): 1/4pi below kappa = 1e-3
-  auto pnorm = [](float k) {
-    return k < 1e-3f ? NMG_INV_4PI : xdiv<FAST>(k * NMG_INV_2PI, one_minus_exp_neg<FAST>(2.f * k));
-  };
-  const float nb = pnorm(kb);
+  const float nb = prod_norm<FAST>(kCosineKappa);
   m.total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    const f3 ma = m.mu[i];
-    const float ka = m.kap[i];
-    f3 nm = add3(scale3(ma, ka), scale3(mb, kb));
-    const float n2 = dot3(nm, nm);
-    float nk;
-    if (FAST) {
-      const float rn = rsqrtf(n2);
-      nk = n2 * rn;
-      if (nk >= 1e-3f) {
-        nm = scale3(nm, rn);
-      } else {
-        nk = 0.f;
-        nm = ma;
-      }
-    } else {
-      nk = sqrtf(n2);
-      if (nk >= 1e-3f) {
-        nm = f3{nm.x / nk, nm.y / nk, nm.z / nk};
-      } else {
-        nk = 0.f;
-        nm = ma;
-      }
-    }
-    const float e = xexp<FAST>(ka * (dot3(nm, ma) - 1.f) + kb * (dot3(nm, mb) - 1.f));
-    const float pk = pnorm(nk);
-    // pnorm(ka) equals the lobe's cached vMF normaliser above kappa = 1e-3
-    const float pa = FAST ? (ka < 1e-3f ? NMG_INV_4PI : m.nrm[i]) : pnorm(ka);
-    const float s = xdiv<FAST>(pa * nb, pk) * e;
-    m.lam[i] = s * m.lam[i];
-    m.kap[i] = nk;
-    m.mu[i] = nm;
-    m.nrm[i] = pk;  // equals vmf_norm(nk): nk is 0 or >= 1e-3 here
+    lobe_cosine<FAST>(mb, nb, m.lam[i], m.kap[i], m.mu[i], m.nrm[i]);
     m.total += m.lam[i];
   }
   m.total = fmaxf(m.total, NMG_EPS);

@@ -102,6 +102,25 @@ def test_fused_query_mixture(field, oracle, synth):
         assert np.abs(sel - 1 / (1 + np.exp(-raw[:, 4 * K].astype(np.float64)))).max() < 1e-4
 
 
+def test_fused_query_without_raw_matches_query_with_raw(field, synth):
+    """A query that returns no raw outputs (for 16 lobes: the epilogue that re-reads each lobe group
+    from TMEM instead of holding all raw outputs in registers) returns what the raw-returning query
+    returns: the same lobes, directions and pdfs up to FMA-contraction ulps."""
+    f, _, _ = field
+    perturb(f, 3)
+    q = synth.wavefront(16384, seed=16)
+    pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
+    a = f.query(pos, wo, n, r, u4, want_raw=True)
+    b = f.query(pos, wo, n, r, u4)
+    same = a["lobe"] == b["lobe"]
+    assert float(same.float().mean()) >= 0.9999
+    assert float((a["dir"] - b["dir"])[same].abs().max()) <= 1e-5
+    assert float(((a["pdf"] - b["pdf"]).abs() / a["pdf"])[same].max()) <= 1e-5
+    if f.cfg.selection:
+        assert float((a["selection"] - b["selection"]).abs().max()) <= 1e-6
+    f.check_errors()
+
+
 def test_fused_pdf_at_given_directions(field, oracle, synth):
     """nmg_pdf in one fused pass: at the query's own sampled directions it returns the query's pdf, and at
     arbitrary directions it matches the FP64 mixture on the network's raw outputs; rows past the device
