@@ -78,7 +78,10 @@ static size_t ws_smem_bytes(uint32_t w_bytes) {
          (Cfg::HS ? 0 : Cfg::C * size_t(Sh::TILE_H)) + (2 * Cfg::S + 1 + Cfg::C) * 8 + 16;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, class Cfg>
+// STREAM: the mixture epilogue re-reads the raw outputs from TMEM lobe group
+// by lobe group (query_epilogue_streamed); 16-lobe queries without raw outputs.
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, class Cfg,
+          bool STREAM = false>
 __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid_constant__ FusedArgs a) {
   using Sh = WsShape<F, LEVELS, MODE, SHDEG, BINS>;
   constexpr int NENC = Sh::NENC;
@@ -228,19 +231,30 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
             tc::mma_commit(&done[c]);
           }
         } else {
+          if constexpr (!STREAM) {
 #pragma unroll
-          for (int cc = 0; cc < NOUTMAX / 16; ++cc)
-            if (cc * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + cc * 16, rr + 16 * cc);
-          tc::tmem_wait_ld();
-          tc::fence_before_sync();
+            for (int cc = 0; cc < NOUTMAX / 16; ++cc)
+              if (cc * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + cc * 16, rr + 16 * cc);
+            tc::tmem_wait_ld();
+            tc::fence_before_sync();
+          }
           last_ok = d;
         }
       }
       if (!ok) break;
-      ok = last_ok;  // reconciled across the group at the next tile's barrier
       const long q = tile * kRows + t;
-      if (q < n && ok) {
-        query_epilogue<K, NOUTMAX>(a, q, rr);
+      if constexpr (STREAM) {
+        // warp-collective TMEM reads: the group agrees on ok first, and the accumulator must
+        // outlive every thread's reads, so the group meets again before the next layer 0
+        ok = bar_red_and(bar, kRows, last_ok);
+        if (!ok) break;
+        query_epilogue_streamed<K>(a, q, q < n, lane_addr);
+        tc::fence_before_sync();
+        ok = bar_red_and(bar, kRows, ok);
+        if (!ok) break;
+      } else {
+        ok = last_ok;  // reconciled across the group at the next tile's barrier
+        if (q < n && ok) query_epilogue<K, NOUTMAX>(a, q, rr);
       }
     }
     if (!ok && t == 0) atomicExch(a.err, 6);
@@ -262,9 +276,10 @@ static nmg_status ws_check_regs(Kern kern, int want) {
   return attr.numRegs == want ? NMG_OK : NMG_ERR_UNSUPPORTED;
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, class Cfg>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, class Cfg,
+          bool STREAM = false>
 static nmg_status launch_ws(const FusedArgs& a, cudaStream_t st) {
-  auto kern = k_fused_query_ws<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, Cfg>;
+  auto kern = k_fused_query_ws<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, Cfg, STREAM>;
   static int regs_ok = 0;  // 1: checked and usable, -1: unusable
   if (regs_ok == 0) regs_ok = ws_check_regs(kern, Cfg::RL) == NMG_OK ? 1 : -1;
   if (regs_ok < 0)
@@ -294,7 +309,9 @@ static nmg_status launch_ws_tiling(int tiling, const FusedArgs& a, cudaStream_t 
 nmg_status launch_query_ws(int preset, int tiling, const FusedArgs& a, cudaStream_t st) {
   switch (preset) {
     case 1: return launch_ws_tiling<2, 16, 1, 4, 4, 8, 48, false>(tiling, a, st);
-    case 2: return launch_ws<2, 16, 1, 4, 4, 16, 80, false, WsE4C2>(a, st);
+    case 2:
+      if (!a.raw && !a.raw_mode) return launch_ws<2, 16, 1, 4, 4, 16, 80, false, WsE4C2, true>(a, st);
+      return launch_ws<2, 16, 1, 4, 4, 16, 80, false, WsE4C2>(a, st);
     case 3: return launch_ws_tiling<4, 8, 0, 2, 4, 8, 48, true>(tiling, a, st);
   }
   return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
