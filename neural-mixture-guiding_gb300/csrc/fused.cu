@@ -104,7 +104,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
       else
         featurize<true>(a.enc, load3(a.pos, q), load3(a.wo, q), load3(a.nrm, q), a.rough[q], x);
     }
-    encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH>(a, x, A, t);
+    encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, true, true>(a, x, A, t);
     tc::fence_proxy_async();
     tc::fence_before_sync();
     ok = bar_red_and(1 + wg, kRows, ok);

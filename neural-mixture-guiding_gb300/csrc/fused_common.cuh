@@ -124,8 +124,9 @@ NMG_D void load_feats(const uint16_t* table, uint32_t entry, float* v, bool fp16
 // (w_x' * w_y') * w_z' as in the reference. PAIR (F = 2): the x and x+1
 // corners of a (y, z) pair that share an aligned 8-byte word (every other
 // cell: for dense levels e1 = e0 + 1, for hashed ones e1 = e0 ^ 1 when x is
-// even) are read with one 8-byte load -- a quarter fewer L1 requests in
-// the query kernel's encoders (648 instead of 678 us); the training kernel,
+// even) are read with one 8-byte load -- a quarter fewer L1 requests: the
+// query kernels take 648 instead of 678 us (warp-specialised) and 797
+// instead of 834 us (one pipeline per warpgroup); the training kernel,
 // whose compute warpgroups gather with more registers, measured 1% slower
 // with it.
 template <int F, bool SMOOTH, bool PAIR = false>
