@@ -30,8 +30,9 @@ namespace nmg {
 // chunk is one more launch of the persistent query kernel, whose pipeline
 // fill and last-round imbalance cost ~19 us per launch: a 1920x1080 query
 // pass plus training step on host buffers measured 1.39 ms with 4 chunks,
-// 1.41 with 2, 1.42 with 7 and 1.58 with 15. Below about 2^18 queries a
-// chunk leaves the persistent grid underfilled.
+// 1.41 with 2, 1.42 with 7 and 1.58 with 15 (even chunks), and 1.32 ms once
+// the last of 4 chunks is half the size of the others. Below about 2^18
+// queries a chunk leaves the persistent grid underfilled.
 constexpr int kMaxChunks = 4;
 constexpr int kMinChunk = 1 << 18;
 
@@ -186,10 +187,14 @@ nmg_status nmg_query_host(nmg_ctx* c, const nmg_shading* in, const float* u4, in
   NMG_CU(cudaStreamWaitEvent(h->d2h, h->start, 0));
   int chunks = n / kMinChunk;
   chunks = chunks < 1 ? 1 : (chunks > kMaxChunks ? kMaxChunks : chunks);
-  const int per = (n + chunks - 1) / chunks;
+  // the last chunk's outputs are copied back after every kernel has run, so it gets half
+  // an even share and the others split the rest
+  const int last = chunks > 1 ? n / (2 * chunks) : n;
+  const int per = chunks > 1 ? (n - last + chunks - 2) / (chunks - 1) : n;
   for (int i = 0; i < chunks; ++i) {
     const size_t o = size_t(i) * per;
-    const int m = int(size_t(n) - o < size_t(per) ? size_t(n) - o : size_t(per));
+    if (o >= size_t(n)) break;
+    const int m = i == chunks - 1 ? int(size_t(n) - o) : int(size_t(n) - o < size_t(per) ? size_t(n) - o : size_t(per));
     if (m <= 0) break;
     const size_t f = sizeof(float);
     if ((s = h2d(h->pos + 3 * o, in->pos + 3 * o, 3 * f * m, h->h2d)) != NMG_OK ||
