@@ -1,12 +1,13 @@
 """Run the guiding step a few times on a fixed workload, for profilers (ncu).
 
     python neural-mixture-guiding_gb300/profile_step.py [--path bf16|fp16|fp32]
-        [--queries N] [--train N] [--repeat R] [--mixture N]
+        [--queries N] [--train N] [--repeat R] [--mixture N] [--tiling T]
 
 Builds one guiding field (hash-grid network), runs R query passes over an N-query
 synthetic wavefront and, with --train, R training steps of that many records.
 With --mixture N it runs the mixture-only kernels instead (R x sample, pdf and
-loss/gradient on N synthetic raw rows, K = --lobes).
+loss/gradient on N synthetic raw rows, K = --lobes). --tiling selects the query
+kernel's tiling (nmg_set_query_tiling; 0 = the default).
 Prints "ok" on success. Nothing is timed here: profile with e.g.
     ncu --set full --clock-control none -k regex:k_fused_query -s 2 -c 1 -o prof \\
         python neural-mixture-guiding_gb300/profile_step.py
@@ -31,6 +32,7 @@ def main():
     ap.add_argument("--repeat", type=int, default=3)
     ap.add_argument("--lobes", type=int, default=8)
     ap.add_argument("--mixture", type=int, default=0)
+    ap.add_argument("--tiling", type=int, default=0)
     args = ap.parse_args()
     import torch
 
@@ -50,6 +52,7 @@ def main():
     path = {"bf16": nmg.PATH_BF16, "fp16": nmg.PATH_FP16, "fp32": nmg.PATH_FP32}[args.path]
     f = nmg.GuidingField(nmg.config(nmg.PRESET_HASHGRID, path=path, n_lobes=args.lobes),
                          max_queries=args.queries, max_batch=args.train)
+    f.set_query_tiling(args.tiling)
     if args.queries:
         q = synth.wavefront(args.queries, seed=1)
         pos, wo, n, r, u4 = (torch.from_numpy(q[k]).cuda() for k in ("pos", "wo", "normal", "rough", "u4"))
