@@ -456,7 +456,7 @@ def launches_per_step(path):
     return 1 + FUSED_TRAIN_LAUNCHES
 
 
-FUSED_TRAIN_LAUNCHES = 6
+FUSED_TRAIN_LAUNCHES = 5  # k_fused_train, k_step_inc, k_adam_ema, k_finish_stats, k_pack_weights
 
 
 def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):

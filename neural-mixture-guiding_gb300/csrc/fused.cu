@@ -175,7 +175,11 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
 // ------------------------------------------------------------ weight image
 // Element (n, k) of layer l goes to byte layer_off[l] + cm_offset(n, k/8,
 // in_l/8) + 2 (k % 8): each layer becomes a K-major operand of N = out_l rows.
-__global__ void k_pack_weights(PackArgs p, const uint16_t* __restrict__ w16, uint16_t* __restrict__ img) {
+// blockIdx.y selects the image: 0 the training weights, 1 the inference ones.
+__global__ void k_pack_weights(PackArgs p, const uint16_t* __restrict__ w16_train, uint16_t* __restrict__ img_train,
+                               const uint16_t* __restrict__ w16_infer, uint16_t* __restrict__ img_infer) {
+  const uint16_t* __restrict__ w16 = blockIdx.y ? w16_infer : w16_train;
+  uint16_t* __restrict__ img = blockIdx.y ? img_infer : img_train;
   const long total = p.off[p.n_layers];
   for (long i = long(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += long(gridDim.x) * blockDim.x) {
     int l = 0;
@@ -265,8 +269,8 @@ static nmg_status dispatch_query(nmg_ctx* c, const FusedArgs& a, cudaStream_t st
 nmg_status pack_images(nmg_ctx* c, cudaStream_t st) {
   FusedState* s = fstate(c);
   if (!s) return NMG_OK;
-  k_pack_weights<<<64, 256, 0, st>>>(s->pack, c->w16, reinterpret_cast<uint16_t*>(s->img_train));
-  k_pack_weights<<<64, 256, 0, st>>>(s->pack, c->w16_inf, reinterpret_cast<uint16_t*>(s->img_infer));
+  k_pack_weights<<<dim3(64, 2), 256, 0, st>>>(s->pack, c->w16, reinterpret_cast<uint16_t*>(s->img_train), c->w16_inf,
+                                              reinterpret_cast<uint16_t*>(s->img_infer));
   return check_launch("k_pack_weights");
 }
 
