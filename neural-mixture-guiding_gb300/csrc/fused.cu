@@ -418,7 +418,7 @@ static std::string tune_key(nmg_ctx* c, int n) {
   cudaGetDeviceProperties(&prop, c->device);
   int bucket = 0;
   while ((1 << (bucket + 1)) <= n) ++bucket;  // log2 size class
-  char buf[256];
+  char buf[384];  // the device name alone can take 256 bytes
   snprintf(buf, sizeof(buf), "%s|sm%d%d|preset%d|fp16=%d|n2^%d", prop.name, prop.major, prop.minor, fstate(c)->preset,
            c->cfg.path == NMG_PATH_FP16, bucket);
   for (char* q = buf; *q; ++q)
