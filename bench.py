@@ -402,13 +402,15 @@ class L2Flush:
 
 def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
     """The mixture-only workload (K = 8 raw outputs per query, no network) at a size whose traffic
-    dwarfs L2, 2^21 queries: sample+pdf and KL loss+gradient, CUDA events, L2 flushed.
-    Algorithmic bytes per query: 164 (raw 128 + uniforms 16 in; direction 12, pdf 4, lobe 4 out) and
-    284 (raw 128 + record 28 in; gradient 128 out)."""
+    dwarfs L2, 2^21 queries: sample+pdf, pdf at given directions (the MIS pdf) and KL loss+gradient,
+    CUDA events, L2 flushed. Algorithmic bytes per query: 164 (raw 128 + uniforms 16 in; direction 12,
+    pdf 4, lobe 4 out), 144 (raw 128 + direction 12 in; pdf 4 out) and 284 (raw 128 + record 28 in;
+    gradient 128 out)."""
     raw, u4, rec = synth.mixture_batch(n, K, seed=7272, selection=False)
     r, u, rc = (torch.from_numpy(a).cuda() for a in (raw, u4, rec))
     d = torch.empty((n, 3), device="cuda")
     p = torch.empty(n, device="cuda")
+    p2 = torch.empty(n, device="cuda")
     lb = torch.empty(n, device="cuda", dtype=torch.int32)
     g = torch.empty_like(r)
     lib = nmg.lib()
@@ -423,13 +425,17 @@ def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
         nmg.check(lib.nmg_mixture_sample(ctypes.byref(opts), ptr(r), ptr(u), None, n, ptr(d), ptr(p), ptr(lb),
                                          ctypes.c_void_p(st.cuda_stream)))
 
+    def pdf():  # at the directions sample() drew
+        nmg.check(lib.nmg_mixture_pdf(ctypes.byref(opts), ptr(r), ptr(d), None, n, ptr(p2),
+                                      ctypes.c_void_p(st.cuda_stream)))
+
     def loss():
         nmg.check(lib.nmg_mixture_loss_grad(ctypes.byref(opts), ptr(r), ptr(rc), rc.shape[1], n, ctypes.c_float(128.0),
                                             ptr(g), None, ptr(tot), ptr(ws), ctypes.c_size_t(ws_bytes),
                                             ctypes.c_void_p(st.cuda_stream)))
 
     out = {"queries": n, "K": K, "l2": "flushed before each timed launch (256 MiB write, then a 256 MiB read)"}
-    for name, fn, per in (("sample_pdf", sample, 164), ("loss_grad", loss, 284)):
+    for name, fn, per in (("sample_pdf", sample, 164), ("pdf", pdf, 144), ("loss_grad", loss, 284)):
         for _ in range(3):
             fn()
         ts = []

@@ -73,17 +73,124 @@ NMG_HD void sincospi_poly(float t, float* s, float* c) {
   *c = hi ? -ca : ca;
 }
 
+// sin(pi k/32) and cos(pi k/32) for k = 0..64, each rounded once to FP32
+// from an 80-bit long-double evaluation (the multiples of 1/2 are exact).
+#define NMG_SINCOSPI32_TABLE { \
+  {0.000000000e+00f, 1.000000000e+00f}, /* k = 0 */ \
+  {9.801714122e-02f, 9.951847196e-01f}, /* k = 1 */ \
+  {1.950903237e-01f, 9.807852507e-01f}, /* k = 2 */ \
+  {2.902846634e-01f, 9.569403529e-01f}, /* k = 3 */ \
+  {3.826834261e-01f, 9.238795042e-01f}, /* k = 4 */ \
+  {4.713967443e-01f, 8.819212914e-01f}, /* k = 5 */ \
+  {5.555702448e-01f, 8.314695954e-01f}, /* k = 6 */ \
+  {6.343932748e-01f, 7.730104327e-01f}, /* k = 7 */ \
+  {7.071067691e-01f, 7.071067691e-01f}, /* k = 8 */ \
+  {7.730104327e-01f, 6.343932748e-01f}, /* k = 9 */ \
+  {8.314695954e-01f, 5.555702448e-01f}, /* k = 10 */ \
+  {8.819212914e-01f, 4.713967443e-01f}, /* k = 11 */ \
+  {9.238795042e-01f, 3.826834261e-01f}, /* k = 12 */ \
+  {9.569403529e-01f, 2.902846634e-01f}, /* k = 13 */ \
+  {9.807852507e-01f, 1.950903237e-01f}, /* k = 14 */ \
+  {9.951847196e-01f, 9.801714122e-02f}, /* k = 15 */ \
+  {1.000000000e+00f, 0.000000000e+00f}, /* k = 16 */ \
+  {9.951847196e-01f, -9.801714122e-02f}, /* k = 17 */ \
+  {9.807852507e-01f, -1.950903237e-01f}, /* k = 18 */ \
+  {9.569403529e-01f, -2.902846634e-01f}, /* k = 19 */ \
+  {9.238795042e-01f, -3.826834261e-01f}, /* k = 20 */ \
+  {8.819212914e-01f, -4.713967443e-01f}, /* k = 21 */ \
+  {8.314695954e-01f, -5.555702448e-01f}, /* k = 22 */ \
+  {7.730104327e-01f, -6.343932748e-01f}, /* k = 23 */ \
+  {7.071067691e-01f, -7.071067691e-01f}, /* k = 24 */ \
+  {6.343932748e-01f, -7.730104327e-01f}, /* k = 25 */ \
+  {5.555702448e-01f, -8.314695954e-01f}, /* k = 26 */ \
+  {4.713967443e-01f, -8.819212914e-01f}, /* k = 27 */ \
+  {3.826834261e-01f, -9.238795042e-01f}, /* k = 28 */ \
+  {2.902846634e-01f, -9.569403529e-01f}, /* k = 29 */ \
+  {1.950903237e-01f, -9.807852507e-01f}, /* k = 30 */ \
+  {9.801714122e-02f, -9.951847196e-01f}, /* k = 31 */ \
+  {0.000000000e+00f, -1.000000000e+00f}, /* k = 32 */ \
+  {-9.801714122e-02f, -9.951847196e-01f}, /* k = 33 */ \
+  {-1.950903237e-01f, -9.807852507e-01f}, /* k = 34 */ \
+  {-2.902846634e-01f, -9.569403529e-01f}, /* k = 35 */ \
+  {-3.826834261e-01f, -9.238795042e-01f}, /* k = 36 */ \
+  {-4.713967443e-01f, -8.819212914e-01f}, /* k = 37 */ \
+  {-5.555702448e-01f, -8.314695954e-01f}, /* k = 38 */ \
+  {-6.343932748e-01f, -7.730104327e-01f}, /* k = 39 */ \
+  {-7.071067691e-01f, -7.071067691e-01f}, /* k = 40 */ \
+  {-7.730104327e-01f, -6.343932748e-01f}, /* k = 41 */ \
+  {-8.314695954e-01f, -5.555702448e-01f}, /* k = 42 */ \
+  {-8.819212914e-01f, -4.713967443e-01f}, /* k = 43 */ \
+  {-9.238795042e-01f, -3.826834261e-01f}, /* k = 44 */ \
+  {-9.569403529e-01f, -2.902846634e-01f}, /* k = 45 */ \
+  {-9.807852507e-01f, -1.950903237e-01f}, /* k = 46 */ \
+  {-9.951847196e-01f, -9.801714122e-02f}, /* k = 47 */ \
+  {-1.000000000e+00f, 0.000000000e+00f}, /* k = 48 */ \
+  {-9.951847196e-01f, 9.801714122e-02f}, /* k = 49 */ \
+  {-9.807852507e-01f, 1.950903237e-01f}, /* k = 50 */ \
+  {-9.569403529e-01f, 2.902846634e-01f}, /* k = 51 */ \
+  {-9.238795042e-01f, 3.826834261e-01f}, /* k = 52 */ \
+  {-8.819212914e-01f, 4.713967443e-01f}, /* k = 53 */ \
+  {-8.314695954e-01f, 5.555702448e-01f}, /* k = 54 */ \
+  {-7.730104327e-01f, 6.343932748e-01f}, /* k = 55 */ \
+  {-7.071067691e-01f, 7.071067691e-01f}, /* k = 56 */ \
+  {-6.343932748e-01f, 7.730104327e-01f}, /* k = 57 */ \
+  {-5.555702448e-01f, 8.314695954e-01f}, /* k = 58 */ \
+  {-4.713967443e-01f, 8.819212914e-01f}, /* k = 59 */ \
+  {-3.826834261e-01f, 9.238795042e-01f}, /* k = 60 */ \
+  {-2.902846634e-01f, 9.569403529e-01f}, /* k = 61 */ \
+  {-1.950903237e-01f, 9.807852507e-01f}, /* k = 62 */ \
+  {-9.801714122e-02f, 9.951847196e-01f}, /* k = 63 */ \
+  {0.000000000e+00f, 1.000000000e+00f}, /* k = 64 */ \
+}
+
+// sin(pi t) and cos(pi t) for t in [0, 2] from that table: t = k/32 + r with
+// k = rint(32 t), where r = t - k/32 is exact and |r| <= 1/64; sin and cos of
+// x = pi r (|x| <= pi/64) by x - x^3/6 and 1 - x^2/2 + x^4/24 (truncation
+// below 2.4e-9 and 2e-11), then the angle-sum formulas. About 16
+// instructions and one 8-byte load against sincospi_poly's ~28, and within
+// 1e-7 of the exact value over [0, 2] (tests/test_sincospi_host.py).
+NMG_HD void sincospi_tab(const float2* tab, float t, float* s, float* c) {
+  const float kf = rintf(32.f * t);
+  int k = int(kf);
+  k = k < 0 ? 0 : (k > 64 ? 64 : k);
+  const float x = fmaf(kf, -1.f / 32.f, t) * NMG_PI, x2 = x * x;
+  const float sr = fmaf(x * x2, -1.f / 6.f, x);
+  const float cr = fmaf(x2, fmaf(x2, 1.f / 24.f, -0.5f), 1.f);
+  const float2 a = tab[k];
+  *s = fmaf(a.x, cr, a.y * sr);
+  *c = fmaf(a.y, cr, -(a.x * sr));
+}
+
+// The table in constant memory and the per-block copy the kernels index (a
+// warp's 32 different indices into constant memory would serialise).
+// A kernel that evaluates angles with kAngTab calls sincospi_tab_fill() once
+// at its start, before any thread can leave.
+static __constant__ float2 c_sincospi32[65] = NMG_SINCOSPI32_TABLE;
+static __shared__ float2 s_sincospi32[65];
+NMG_D void sincospi_tab_fill() {
+  for (int i = threadIdx.x; i < 65; i += blockDim.x) s_sincospi32[i] = c_sincospi32[i];
+  __syncthreads();
+}
+
+// How lobe_angles evaluates sin/cos: the hardware approximation, the folded
+// polynomial, or the shared-memory table.
+enum : int { kAngHw = 0, kAngPoly = 1, kAngTab = 2 };
+
 // sin/cos of the lobe angles theta = pi * st and phi = 2 pi * sp (st, sp the
-// logistic outputs in (0, 1)). PRECISE evaluates them at pi * t without
-// rounding pi * t first (sincospi_poly), keeping the mean direction to
-// ~1e-7; the hardware approximation (FAST and not PRECISE) is off by up to
+// logistic outputs in (0, 1)). PRECISE (kAngPoly, kAngTab) evaluates them at
+// pi * t without rounding pi * t first (sincospi_poly, or sincospi_tab from
+// the block's shared table), keeping the mean direction to ~1e-7; the
+// hardware approximation (kAngHw: FAST and not PRECISE) is off by up to
 // ~4e-7, which a lobe of concentration kappa turns into a relative pdf
 // error of ~4e-7 kappa.
 // FOLD01 = false keeps the general fold for theta as well (shorter code is
 // not always faster: it changes the register allocation of the caller).
-template <bool FAST, bool PRECISE, bool FOLD01 = true>
+template <bool FAST, int PRECISE, bool FOLD01 = true>
 NMG_D void lobe_angles(float st, float sp, float* sth, float* cth, float* sph, float* cph) {
-  if (PRECISE) {
+  if (PRECISE == kAngTab) {
+    sincospi_tab(s_sincospi32, st, sth, cth);
+    sincospi_tab(s_sincospi32, 2.f * sp, sph, cph);
+  } else if (PRECISE) {
     sincospi_poly<!FOLD01>(st, sth, cth);
     sincospi_poly<true>(2.f * sp, sph, cph);
   } else {
@@ -145,7 +252,7 @@ template <bool FAST> NMG_D float vmf_norm(float k) {
 
 // distribution.h:85-98: activation of one query's raw outputs. `raw` points
 // at 4K floats (lambda, kappa, theta, phi per lobe), 16-byte aligned.
-template <int K, bool FAST, bool PRECISE = !FAST>
+template <int K, bool FAST, int PRECISE = !FAST>
 NMG_D void mix_activate(Mix<K>& m, const float* raw, int kappa_softplus) {
   m.total = 0.f;
 #pragma unroll
@@ -367,7 +474,7 @@ NMG_D float raw_at(const float (&raw)[N], int i) { return raw[i < N ? i : 0]; }
 // dF/dlambda uses the O(K) form (vmf_s - q)/total, algebraically equal to
 // the reference's O(K^2) sum. NaN/Inf gradients become 0 and gradients are
 // clamped above at 150 (train.cu:109-123). Returns the per-sample loss.
-template <int K, bool FAST, bool PRECISE = !FAST, class RAW>
+template <int K, bool FAST, int PRECISE = !FAST, class RAW>
 NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, const MixOpts& o, float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];
   float total = 0.f;
@@ -443,7 +550,7 @@ NMG_D float mix_kl_loss_grad(const RAW& raw, const float* rec, float scale, cons
 // train.cu:126-172: the learned-selection variant. raw[4K] is the selection
 // logit; rec[6] the BSDF pdf of the direction. No NaN/clamp post-pass
 // (the reference has none for this variant). grad has 4K+1 entries.
-template <int K, bool FAST, bool PRECISE = !FAST, class RAW>
+template <int K, bool FAST, int PRECISE = !FAST, class RAW>
 NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float scale, const MixOpts& o,
                                        float* grad) {
   float lam[K], kap[K], sth[K], cth[K], sph[K], cph[K], sgt[K], sgp[K], dkap[K];

@@ -8,6 +8,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "api_common.cuh"
@@ -42,22 +43,91 @@ static int grid_for(long n) {
   return int(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
 }
 
+// One wave of the blocks that fit on the device at once (a persistent grid:
+// the staged kernels overlap each thread's next copies with its current
+// query, which pays only over many queries per thread), or fewer for small n.
+template <class Kern>
+static int resident_grid(Kern kernel, int smem, long n) {
+  int dev = 0, sms = 152, per_sm = 1;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  const long blocks = (n + kThreads - 1) / kThreads, cap = long(sms) * per_sm;
+  return int(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
+}
+
+// Per-thread asynchronous copies global -> shared (cp.async, bypassing L1):
+// a thread stages the rows of its next query while it computes the current
+// one, and waits only for its own copies (cp.async.wait_group), so no block
+// barrier and no spin-wait is involved.
+NMG_D uint32_t shared_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
+NMG_D void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(shared_u32(smem)), "l"(gmem) : "memory");
+}
+NMG_D void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(shared_u32(smem)), "l"(gmem) : "memory");
+}
+NMG_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N> NMG_D void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// Double-buffered staging fits the 48 KB of dynamic shared memory a launch
+// gets without opting in: 2 x 128 threads x `per_thread` bytes.
+constexpr bool stage_fits(int per_thread) { return 2 * kThreads * per_thread <= 48 * 1024; }
+
+// Raw row (K float4) and uniforms (one float4) of query q into `dst`, as one
+// commit group (empty past the end, so that the group count stays uniform).
+template <int K>
+NMG_D void stage_sample_row(float4* dst, const float* raw, int stride, const float* u4, long q, int n) {
+  if (q < n) {
+#pragma unroll
+    for (int i = 0; i < K; ++i) cp_async16(dst + i, raw + q * stride + 4 * i);
+    cp_async16(dst + K, u4 + 4 * q);
+  }
+  cp_async_commit();
+}
+
 template <int K, bool FAST>
-__global__ void __launch_bounds__(kThreads) k_mixture_sample(const float* __restrict__ raw, int stride,
+NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int kappa_softplus, float* dir,
+                      float* pdf, int* lobe) {
+  Mix<K> m;
+  mix_activate<K, FAST, kAngTab>(m, row, kappa_softplus);
+  if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
+  int sel = mix_select<K>(m, u.y);
+  f3 d = mix_sample_lobe<K, FAST>(m, sel, u.z, u.w);
+  store3(dir, q, d);
+  pdf[q] = mix_pdf<K, FAST>(m, d);
+  if (lobe) lobe[q] = sel;
+}
+
+// STAGED: rows pass through shared memory (dynamic, 2 x kThreads x (K + 1)
+// float4), the next query's copies in flight during the current query's
+// arithmetic; otherwise direct 128-bit loads (K = 16, whose staging would
+// need more than 48 KB).
+template <int K, bool FAST, bool STAGED>
+__global__ void __launch_bounds__(kThreads, STAGED ? 6 : 1) k_mixture_sample(const float* __restrict__ raw, int stride,
                                                              const float* __restrict__ u4,
                                                              const float* __restrict__ cosn, int n,
                                                              int kappa_softplus, float* __restrict__ dir,
                                                              float* __restrict__ pdf, int* __restrict__ lobe) {
-  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
-    Mix<K> m;
-    mix_activate<K, FAST, true>(m, raw + q * stride, kappa_softplus);
-    if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
-    float4 u = reinterpret_cast<const float4*>(u4)[q];
-    int sel = mix_select<K>(m, u.y);
-    f3 d = mix_sample_lobe<K, FAST>(m, sel, u.z, u.w);
-    store3(dir, q, d);
-    pdf[q] = mix_pdf<K, FAST>(m, d);
-    if (lobe) lobe[q] = sel;
+  sincospi_tab_fill();
+  const long step = long(gridDim.x) * blockDim.x;
+  long q = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  if constexpr (STAGED) {
+    constexpr int R = K + 1, kStage = kThreads * R;
+    extern __shared__ float4 s_stage[];
+    float4* mine = s_stage + threadIdx.x * R;
+    stage_sample_row<K>(mine, raw, stride, u4, q, n);
+    for (int s = 0; q < n; q += step, s ^= 1) {
+      stage_sample_row<K>(mine + (s ^ 1) * kStage, raw, stride, u4, q + step, n);
+      cp_async_wait<1>();  // this thread's copies for query q have landed
+      const float4* row = mine + s * kStage;
+      sample_one<K, FAST>(reinterpret_cast<const float*>(row), row[K], cosn, q, kappa_softplus, dir, pdf, lobe);
+    }
+    cp_async_wait<0>();
+  } else {
+    for (; q < n; q += step)
+      sample_one<K, FAST>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
+                          pdf, lobe);
   }
 }
 
@@ -66,9 +136,10 @@ __global__ void __launch_bounds__(kThreads) k_mixture_pdf(const float* __restric
                                                           const float* __restrict__ wi,
                                                           const float* __restrict__ cosn, int n,
                                                           int kappa_softplus, float* __restrict__ pdf) {
+  sincospi_tab_fill();
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
     Mix<K> m;
-    mix_activate<K, FAST, true>(m, raw + q * stride, kappa_softplus);
+    mix_activate<K, FAST, kAngTab>(m, raw + q * stride, kappa_softplus);
     if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
     pdf[q] = mix_pdf<K, FAST>(m, load3(wi, q));
   }
@@ -96,14 +167,15 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad(const float* __r
                                                                 float* __restrict__ grad,
                                                                 float* __restrict__ loss,
                                                                 double* __restrict__ partials) {
+  sincospi_tab_fill();
   double acc = 0.0;
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
     float r[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
     float g[4 * K + 1];
-    float l = SEL ? mix_kl_loss_grad_selection<K, kMixFast, true>(raw + q * stride, r, scale, o, g)
-                  : mix_kl_loss_grad<K, kMixFast, true>(raw + q * stride, r, scale, o, g);
+    float l = SEL ? mix_kl_loss_grad_selection<K, kMixFast, kAngTab>(raw + q * stride, r, scale, o, g)
+                  : mix_kl_loss_grad<K, kMixFast, kAngTab>(raw + q * stride, r, scale, o, g);
     float4* gr = reinterpret_cast<float4*>(grad + q * stride);
 #pragma unroll
     for (int i = 0; i < K; ++i) gr[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
@@ -142,9 +214,9 @@ NMG_D void pair_weights(Mix<KH>& m, float total) {
 }
 
 template <int K, bool FAST>
-NMG_D void pair_mixture(Mix<K / 2>& m, const float* row, const float* cosn, long q, int h, int kappa_softplus) {
+NMG_D void pair_mixture(Mix<K / 2>& m, const float* half_row, const float* cosn, long q, int kappa_softplus) {
   constexpr int KH = K / 2;
-  mix_activate<KH, FAST, true>(m, row + h * KH * 4, kappa_softplus);
+  mix_activate<KH, FAST, kAngTab>(m, half_row, kappa_softplus);
   float lt = 0.f;
 #pragma unroll
   for (int i = 0; i < KH; ++i) lt += m.lam[i];
@@ -158,26 +230,82 @@ NMG_D void pair_mixture(Mix<K / 2>& m, const float* row, const float* cosn, long
   }
 }
 
-template <int K, bool FAST>
+// Lane h's half row (KH float4) and the direction (3 floats, 4-byte copies)
+// of the query of thread index t, as one commit group (empty past the end).
+template <int KH>
+NMG_D void stage_pdf_row(float4* dst, const float* raw, int stride, const float* wi, long t, int n, int h) {
+  const long q = t >> 1;
+  if (q < n) {
+#pragma unroll
+    for (int i = 0; i < KH; ++i) cp_async16(dst + i, raw + q * stride + h * KH * 4 + 4 * i);
+    float* wd = reinterpret_cast<float*>(dst + KH);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) cp_async4(wd + j, wi + 3 * q + j);
+  }
+  cp_async_commit();
+}
+
+// STAGED: as the loss kernel, half rows and directions through shared memory
+// (2 x kThreads x (KH + 1) float4), one wave of resident blocks.
+template <int K, bool FAST, bool STAGED = false>
 __global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restrict__ raw, int stride,
                                                            const float* __restrict__ wi,
                                                            const float* __restrict__ cosn, int n,
                                                            int kappa_softplus, float* __restrict__ pdf) {
-  constexpr int KH = K / 2;
+  constexpr int KH = K / 2, R = KH + 1, kStage = kThreads * R;
   const int h = threadIdx.x & 1;
-  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += long(gridDim.x) * blockDim.x) {
+  sincospi_tab_fill();
+  const long step = long(gridDim.x) * blockDim.x;
+  long t = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  extern __shared__ float4 s_stage[];
+  float4* mine = s_stage + threadIdx.x * R;
+  if constexpr (STAGED) stage_pdf_row<KH>(mine, raw, stride, wi, t, n, h);
+  for (int sb = 0; (t >> 1) < n; t += step, sb ^= 1) {
     const long q = t >> 1;
     Mix<KH> m;
-    pair_mixture<K, FAST>(m, raw + q * stride, cosn, q, h, kappa_softplus);
-    const float p = pair_sum(mix_pdf<KH, FAST>(m, load3(wi, q)));
+    float p;
+    if constexpr (STAGED) {
+      stage_pdf_row<KH>(mine + (sb ^ 1) * kStage, raw, stride, wi, t + step, n, h);
+      cp_async_wait<1>();  // this lane's copies for query q have landed
+      const float4* st4 = mine + sb * kStage;
+      pair_mixture<K, FAST>(m, reinterpret_cast<const float*>(st4), cosn, q, kappa_softplus);
+      const float4 w = st4[KH];
+      p = pair_sum(mix_pdf<KH, FAST>(m, f3{w.x, w.y, w.z}));
+    } else {
+      pair_mixture<K, FAST>(m, raw + q * stride + h * KH * 4, cosn, q, kappa_softplus);
+      p = pair_sum(mix_pdf<KH, FAST>(m, load3(wi, q)));
+    }
     if (h == 0) pdf[q] = p;
   }
+  if constexpr (STAGED) cp_async_wait<0>();
+}
+
+// Lane h's half row (KH float4) and the whole record (up to 8 floats, 4-byte
+// copies: records are 24 or 28 bytes) of the query of thread index t, as one
+// commit group (empty past the end).
+template <int KH>
+NMG_D void stage_loss_row(float4* dst, const float* raw, int stride, const float* rec, int rstride, long t, int n,
+                          int h) {
+  const long q = t >> 1;
+  if (q < n) {
+#pragma unroll
+    for (int i = 0; i < KH; ++i) cp_async16(dst + i, raw + q * stride + h * KH * 4 + 4 * i);
+    float* rd = reinterpret_cast<float*>(dst + KH);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      if (j < rstride) cp_async4(rd + j, rec + q * rstride + j);
+  }
+  cp_async_commit();
 }
 
 // train.cu:69-172 with the lobes split over a lane pair: each lane computes
 // its lobes' activations, vMF values and gradients; q and the total come
 // from the pair's partial sums.
-template <int K, bool SEL>
+// STAGED: each lane's half row and the record pass through shared memory
+// (dynamic, 2 x kThreads x (KH + 2) float4), the next query's copies in
+// flight during the current one's arithmetic (launched as one wave of
+// resident blocks); otherwise direct loads.
+template <int K, bool SEL, bool STAGED = false>
 __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __restrict__ raw, int stride,
                                                                  const float* __restrict__ rec, int rstride, int n,
                                                                  float scale, MixOpts o, float* __restrict__ grad,
@@ -185,18 +313,36 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
                                                                  double* __restrict__ partials) {
   constexpr int KH = K / 2;
   constexpr bool FAST = kMixFast;
+  constexpr int R = KH + 2, kStage = kThreads * R;  // float4 per lane: its lobes, the record
   const int h = threadIdx.x & 1;
+  sincospi_tab_fill();
   double acc = 0.0;
-  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += long(gridDim.x) * blockDim.x) {
+  const long step = long(gridDim.x) * blockDim.x;
+  long t = long(blockIdx.x) * blockDim.x + threadIdx.x;
+  extern __shared__ float4 s_stage[];
+  float4* mine = s_stage + threadIdx.x * R;
+  if constexpr (STAGED) stage_loss_row<KH>(mine, raw, stride, rec, rstride, t, n, h);
+  for (int sb = 0; (t >> 1) < n; t += step, sb ^= 1) {
     const long q = t >> 1;
     float r[8];
+    const float* row;
+    if constexpr (STAGED) {
+      stage_loss_row<KH>(mine + (sb ^ 1) * kStage, raw, stride, rec, rstride, t + step, n, h);
+      cp_async_wait<1>();  // this lane's copies for query q have landed
+      const float4* st4 = mine + sb * kStage;
+      row = reinterpret_cast<const float*>(st4);
+      const float* rs = reinterpret_cast<const float*>(st4 + KH);
 #pragma unroll
-    for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
+      for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rs[j] : 0.f;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
+      row = raw + q * stride + h * KH * 4;
+    }
     float swt, cwt, swp, cwp;
     sincosf(r[0], &swt, &cwt);
     sincosf(r[1], &swp, &cwp);
     const f3 wi{swt * cwp, swt * swp, cwt};
-    const float* row = raw + q * stride + h * KH * 4;
     float lam[KH], kap[KH], dkap[KH], vmf[KH], cc[KH], dta[KH], dpa[KH], sgt[KH], sgp[KH];
     float lt = 0.f, nt = 0.f;
 #pragma unroll
@@ -213,7 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       sgt[i] = logistic<FAST>(x.z);
       sgp[i] = logistic<FAST>(x.w);
       float sth, cth, sph, cph;
-      lobe_angles<FAST, true, false>(sgt[i], sgp[i], &sth, &cth, &sph, &cph);
+      lobe_angles<FAST, kAngTab, false>(sgt[i], sgp[i], &sth, &cth, &sph, &cph);
       cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
       dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
       dpa[i] = (wi.y * cph - wi.x * sph) * sth;
@@ -223,7 +369,8 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       nt += lam[i] * vmf[i];
     }
     const float total = pair_sum(lt);
-    const float qv = pair_sum(nt) / total;
+    const float inv_total = 1.f / total;
+    const float qv = pair_sum(nt) * inv_total;
     const float Li = (r[2] + (r[3] + r[4])) / 3.f;
     float prefix, l, sel = 1.f;
     if (SEL) {
@@ -236,7 +383,6 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       prefix = -Li / wp / guide * scale;
       l = -Li / wp * logf(guide);
     }
-    const float inv_total = 1.f / total;
     float4* gr = reinterpret_cast<float4*>(grad + q * stride) + h * KH;
 #pragma unroll
     for (int i = 0; i < KH; ++i) {
@@ -249,7 +395,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
         ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
       } else {
         const float e = xexp<FAST>(-2.f * k);
-        ik = 1.f / k - (1.f + e) / (1.f - e);
+        ik = xdiv<FAST>(1.f, k) - xdiv<FAST>(1.f + e, 1.f - e);
       }
       float g0 = prefix * ((vmf[i] - qv) * inv_total * sel) * lam[i];
       float g1 = prefix * (wv * (cc[i] + ik) * sel) * dkap[i];
@@ -269,6 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       acc += double(l);
     }
   }
+  if constexpr (STAGED) cp_async_wait<0>();
   const double s = block_sum_fixed(acc);
   if (threadIdx.x == 0 && partials) partials[blockIdx.x] = s;
 }
@@ -278,17 +425,26 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
                                 int n, float* dir, float* pdf, int* lobe, cudaStream_t st) {
   // one thread per query: splitting the lobes over a lane pair (as the loss does) measured slower here,
   // the selection and the sampling of the chosen lobe being per-query work both lanes would repeat
-  k_mixture_sample<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
-                                                               dir, pdf, lobe);
+  constexpr int per_thread = (K + 1) * 16;
+  constexpr bool staged = stage_fits(per_thread);
+  const int smem = staged ? 2 * kThreads * per_thread : 0;
+  int grid = grid_for(n);
+  if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true>, smem, n);
+  k_mixture_sample<K, kMixFast, staged><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, cosn, n,
+                                                                     o->kappa_softplus, dir, pdf, lobe);
   return check_launch("nmg_mixture_sample");
 }
 
 template <int K>
 static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const float* wi, const float* cosn, int n,
                              float* pdf, cudaStream_t st) {
-  if constexpr (K % 2 == 0)
-    k_mixture_pdf2<K, kMixFast><<<grid_for(2L * n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n,
-                                                                    o->kappa_softplus, pdf);
+  if constexpr (K % 2 == 0) {
+    constexpr int smem = 2 * kThreads * (K / 2 + 1) * 16;
+    static_assert(stage_fits((K / 2 + 1) * 16), "pdf staging above 48 KB");
+    const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true>, smem, 2L * n);
+    k_mixture_pdf2<K, kMixFast, true><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus,
+                                                                    pdf);
+  }
   else
     k_mixture_pdf<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);
   return check_launch("nmg_mixture_pdf");
@@ -299,15 +455,21 @@ static nmg_status launch_loss(const nmg_mixture_opts* o, const float* raw, const
                               float loss_scale, float* grad, float* loss, double* loss_sum, double* partials,
                               cudaStream_t st) {
   MixOpts mo{o->kappa_softplus, o->kappa_poly, 0};
-  const int blocks = grid_for(n);  // the workspace holds one partial per block of this grid
+  int blocks = grid_for(n);  // the workspace holds one partial per block of this grid (at most)
   const float scale = loss_scale / float(n);
   if constexpr (K % 2 == 0) {
-    if (o->selection)
-      k_mixture_loss_grad2<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
-                                                                 loss, loss_sum ? partials : nullptr);
-    else
-      k_mixture_loss_grad2<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
-                                                                  loss, loss_sum ? partials : nullptr);
+    constexpr int smem = 2 * kThreads * (K / 2 + 2) * 16;
+    static_assert(stage_fits((K / 2 + 2) * 16), "loss staging above 48 KB");
+    if (o->selection) {
+      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, true, true>, smem, 2L * n));
+      k_mixture_loss_grad2<K, true, true><<<blocks, kThreads, smem, st>>>(raw, o->stride, rec, rstride, n, scale, mo,
+                                                                         grad, loss, loss_sum ? partials : nullptr);
+    } else {
+      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, false, true>, smem, 2L * n));
+      k_mixture_loss_grad2<K, false, true><<<blocks, kThreads, smem, st>>>(raw, o->stride, rec, rstride, n, scale,
+                                                                          mo, grad, loss,
+                                                                          loss_sum ? partials : nullptr);
+    }
   } else {
     if (o->selection)
       k_mixture_loss_grad<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,

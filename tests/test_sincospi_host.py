@@ -1,12 +1,15 @@
-"""Accuracy of the lobe-mean sine/cosine (csrc/mixture.cuh: sincospi_poly).
+"""Accuracy of the lobe-mean sine/cosine (csrc/mixture.cuh: sincospi_poly
+and sincospi_tab).
 
 The mixture kernels evaluate sin(pi t) and cos(pi t) of the logistic lobe
-angles with their own folded polynomial instead of the hardware
-approximation: an error e in a lobe mean becomes a relative pdf error of
-about e * kappa, so the polynomial must stay within ~1e-7 of the exact value.
-The function is __host__ __device__, so this test compiles a small host
-program against the header with nvcc and compares it with long-double
-sin/cos on a dense grid of float arguments -- on the CPU, no GPU needed.
+angles with their own functions instead of the hardware approximation: the
+plain FP32 path with a folded polynomial, the mixture-only kernels from a
+65-entry table of sin/cos(pi k/32) and short polynomials of the remainder.
+An error e in a lobe mean becomes a relative pdf error of about e * kappa,
+so both must stay within ~1e-7 of the exact value. The functions are
+__host__ __device__, so this test compiles a small host program against the
+header with nvcc and compares them with long-double sin/cos on a dense grid
+of float arguments -- on the CPU, no GPU needed.
 """
 import os
 import shutil
@@ -25,7 +28,8 @@ PROGRAM = r"""
 int main() {
   const long n = 2000000;
   const long double pi = 3.141592653589793238462643383279502884L;
-  double e2 = 0.0, e1 = 0.0;
+  static const float2 tab[65] = NMG_SINCOSPI32_TABLE;
+  double e2 = 0.0, e1 = 0.0, et = 0.0;
   for (long i = 0; i <= n; ++i) {
     // t over [0, 2] (the azimuth argument 2 sp) and over [0, 1] (theta's)
     const float t2 = float(2.0 * double(i) / double(n));
@@ -35,18 +39,27 @@ int main() {
     long double x = (long double)t2 * pi;
     e2 = fmax(e2, double(fabsl((long double)s - sinl(x))));
     e2 = fmax(e2, double(fabsl((long double)c - cosl(x))));
+    nmg::sincospi_tab(tab, t2, &s, &c);
+    et = fmax(et, double(fabsl((long double)s - sinl(x))));
+    et = fmax(et, double(fabsl((long double)c - cosl(x))));
     nmg::sincospi_poly<false>(t1, &s, &c);
     x = (long double)t1 * pi;
     e1 = fmax(e1, double(fabsl((long double)s - sinl(x))));
     e1 = fmax(e1, double(fabsl((long double)c - cosl(x))));
   }
-  printf("%.6e %.6e\n", e2, e1);
+  double ee = 0.0;  // the table entries themselves
+  for (int k = 0; k <= 64; ++k) {
+    const long double x = pi * (long double)k / 32.0L;
+    ee = fmax(ee, double(fabsl((long double)tab[k].x - sinl(x))));
+    ee = fmax(ee, double(fabsl((long double)tab[k].y - cosl(x))));
+  }
+  printf("%.6e %.6e %.6e %.6e\n", e2, e1, et, ee);
   return 0;
 }
 """
 
 
-def test_sincospi_poly_within_1e7(tmp_path):
+def test_sincospi_poly_and_table_within_1e7(tmp_path):
     nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
@@ -56,7 +69,11 @@ def test_sincospi_poly_within_1e7(tmp_path):
     subprocess.run([nvcc, "-std=c++17", "-O2", "-I", CSRC, str(src), "-o", str(exe)], check=True,
                    capture_output=True, timeout=600)
     out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=600).stdout.split()
-    e_two, e_one = float(out[0]), float(out[1])
+    e_two, e_one, e_tab, e_entry = (float(v) for v in out[:4])
     # within 1e-7 of exact over [0, 2] and, without the [1, 2] fold, over [0, 1]
     assert e_two <= 1e-7, e_two
     assert e_one <= 1e-7, e_one
+    # the table form over [0, 2] (its argument range: theta's t in [0, 1], phi's 2 t in [0, 2])
+    assert e_tab <= 1e-7, e_tab
+    # every entry rounded correctly: within half an FP32 ulp of values below 1 (2^-25)
+    assert e_entry <= 2.0 ** -25, e_entry
