@@ -404,7 +404,7 @@ def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
     """The mixture-only workload (K = 8 raw outputs per query, no network) at a size whose traffic
     dwarfs L2, 2^21 queries: sample+pdf, pdf at given directions (the MIS pdf) and KL loss+gradient,
     CUDA events, L2 flushed. Algorithmic bytes per query: 164 (raw 128 + uniforms 16 in; direction 12,
-    pdf 4, lobe 4 out), 144 (raw 128 + direction 12 in; pdf 4 out) and 284 (raw 128 + record 28 in;
+    pdf 4, lobe 4 out), 144 (raw 128 + direction 12 in; pdf 4 out) and 280 (raw 128 + record 24 in;
     gradient 128 out)."""
     raw, u4, rec = synth.mixture_batch(n, K, seed=7272, selection=False)
     r, u, rc = (torch.from_numpy(a).cuda() for a in (raw, u4, rec))
@@ -435,7 +435,7 @@ def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
                                             ctypes.c_void_p(st.cuda_stream)))
 
     out = {"queries": n, "K": K, "l2": "flushed before each timed launch (256 MiB write, then a 256 MiB read)"}
-    for name, fn, per in (("sample_pdf", sample, 164), ("pdf", pdf, 144), ("loss_grad", loss, 284)):
+    for name, fn, per in (("sample_pdf", sample, 164), ("pdf", pdf, 144), ("loss_grad", loss, 280)):
         for _ in range(3):
             fn()
         ts = []
