@@ -174,3 +174,30 @@ def test_softplus_kappa(nmg, oracle, synth):
     g64, _, _ = oracle.mixture_loss_grad(raw, 8, rec, fp64=True, o=oracle.opts(kappa_softplus=1))
     err = np.abs(g.cpu().numpy()[:, :32] - g64[:, :32]).max(axis=1)
     assert np.all(err <= 1e-3 * np.maximum(1.0, np.abs(g64[:, :32]).max(axis=1)))
+
+
+@pytest.mark.parametrize("K", [4, 7, 8])
+def test_lobe_counts_and_ragged_sizes(nmg, oracle, synth, K):
+    """Every compiled lobe count through sample, pdf and loss/gradient at sizes that leave a
+    partial block, a partial lane pair round and a partial last round of the resident grid: the
+    kernels prefetch each thread's next query and must stop at n. Tolerances as above."""
+    raw, u4, rec = synth.mixture_batch(5000, K, seed=21)
+    for n in (1, 129, 5000):
+        check_sample(nmg, oracle, raw[:n], u4[:n], K)
+        wi = synth.uniform_sphere(np.random.default_rng(n), (n,)).astype(np.float32)
+        r, rc, w = to_dev(raw[:n], rec[:n], wi)
+        p = nmg.mixture_pdf(r, w, K).cpu().numpy()
+        p64 = oracle.mixture_pdf(raw[:n], K, wi, fp64=True)
+        # a uniform direction far from every concentrated lobe has a density below FP32's normal
+        # range (e^{kappa (cos - 1)}, kappa up to 1000), which the hardware exponential flushes to 0:
+        # relative error where the density is representable, absolute error below that
+        live = p64 > 1e-20
+        rel = np.abs(p - p64)[live] / p64[live]
+        assert np.all(rel <= 1e-4 + 4e-7 * kappa_max(raw[:n], K, False)[live]), rel.max()
+        assert np.all(np.abs(p - p64)[~live] <= 1e-20)
+        g, loss, tot = nmg.mixture_loss_grad(r, rc, K)
+        g64, l64, t64 = oracle.mixture_loss_grad(raw[:n], K, rec[:n], fp64=True)
+        nout = 4 * K
+        err = np.abs(g.cpu().numpy()[:, :nout] - g64[:, :nout]).max(axis=1)
+        assert np.all(err <= 1e-3 * np.maximum(1.0, np.abs(g64[:, :nout]).max(axis=1))), err.max()
+        assert abs(float(tot.cpu()[0]) - t64) <= 1e-5 * abs(t64) + 1e-6
