@@ -102,7 +102,10 @@ NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int
 // STAGED: rows pass through shared memory (dynamic, 2 x kThreads x (K + 1)
 // float4), the next query's copies in flight during the current query's
 // arithmetic; otherwise direct 128-bit loads (K = 16, whose staging would
-// need more than 48 KB).
+// need more than 48 KB). Staged, 6 blocks per SM are asked for: at K = 8 the
+// staging takes 36 KB per block, so 6 blocks fill the SM's shared memory, and
+// the 80 registers per thread this caps the kernel at (the unstaged kernel's
+// count) leave room for exactly those 6.
 template <int K, bool FAST, bool STAGED>
 __global__ void __launch_bounds__(kThreads, STAGED ? 6 : 1) k_mixture_sample(const float* __restrict__ raw, int stride,
                                                              const float* __restrict__ u4,
