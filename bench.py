@@ -10,8 +10,11 @@ Inputs are seeded synthetic data with the shapes and distributions of that
 workload (neural-mixture-guiding_gb300/synth.py), resident in HBM.
 
 value = guided queries/s of the measured path (default: fused BF16 on
-tcgen05); the same line carries train samples/s and the plain FP32 path's
-numbers measured in the same run. L2 is flushed (a 256 MiB write, then a
+tcgen05) over whole steps: a step's 2,073,600 queries over the time of its
+query pass plus its training step (train_samples_per_s likewise counts the
+step's 2^18 samples over that time); query_pass and train_step give each
+phase's own rate, and plain_fp32 the plain FP32 path's numbers from the same
+run. L2 is flushed (a 256 MiB write, then a
 256 MiB read) before every timed step; each step is timed with CUDA events
 on the launching stream, excluding the flush.
 
@@ -264,22 +267,27 @@ def run_ours(args):
         return
     hbm, bf16, src = peaks()
     steps = args.steps
+    # a step is one query pass over the wavefront plus one training step: the step rates count the
+    # queries and samples of a step over both phases' time; the phase rates over their own phase
+    t_step = ours["t_query"] + ours["t_train"]
+    step_qps, step_tps = ws * N_QUERIES * steps / t_step, ws * N_TRAIN * steps / t_step
     qps = ws * N_QUERIES * steps / ours["t_query"]
     tps = ws * N_TRAIN * steps / ours["t_train"]
     p_steps = max(1, min(args.steps, 3)) if path != nmg.PATH_FP32 else steps
     plain_qps = N_QUERIES * p_steps / plain["t_query"]
     plain_tps = N_TRAIN * p_steps / plain["t_train"]
+    plain_step_qps = N_QUERIES * p_steps / (plain["t_query"] + plain["t_train"])
     tflops = FLOP_PER_QUERY * N_QUERIES / t_kernel / 1e12
     gbs = BYTES_PER_QUERY * N_QUERIES / t_kernel / 1e9
     cpu = cpu_baseline(q, x, rec, seconds=args.cpu_seconds) if not args.no_cpu else None
     line = {
         "metric": "guided queries/s & train samples/s, BF16 fused vs FP32 plain, 1 GB300",
-        "value": qps,
+        "value": step_qps,
         "unit": "queries/s",
         "n_gpus": ws,
         "steps": steps,
         "warmup": args.warmup,
-        "ms_per_step": (ours["t_query"] + ours["t_train"]) / steps * 1e3,
+        "ms_per_step": t_step / steps * 1e3,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
@@ -290,13 +298,19 @@ def run_ours(args):
                               "-> 80-64-64-64-48 MLP, K=8 lobes + selection",
                    "path": args.path, "l2": "flushed before each timed step (256 MiB write, then a 256 MiB read that writes the dirty lines back outside the timed region)",
                    "parallelism": "replicas" if ws > 1 else "single GPU"},
-        "train_samples_per_s": tps,
+        "train_samples_per_s": step_tps,
+        "rates": "value and train_samples_per_s: a step's 2,073,600 queries and 2^18 training samples over the "
+                 "step's time (query pass + training step); query_pass / train_step: each over its own phase",
+        "query_pass": {"queries_per_s": qps, "ms": ours["t_query"] / steps * 1e3},
+        "train_step": {"samples_per_s": tps, "ms": ours["t_train"] / steps * 1e3},
         "query_ms": ours["t_query"] / steps * 1e3,
         "train_ms": ours["t_train"] / steps * 1e3,
-        "plain_fp32": {"queries_per_s": plain_qps, "train_samples_per_s": plain_tps,
+        "plain_fp32": {"step_queries_per_s": plain_step_qps, "query_pass_queries_per_s": plain_qps,
+                       "train_step_samples_per_s": plain_tps,
                        "query_ms": plain["t_query"] / p_steps * 1e3, "train_ms": plain["t_train"] / p_steps * 1e3,
                        "final_stats": {"mean_loss": plain["loss"][0], "grad_norm": plain["loss"][1]}},
-        "speedup_vs_plain_fp32": {"queries": qps / ws / plain_qps, "train": tps / ws / plain_tps},
+        "speedup_vs_plain_fp32": {"step": step_qps / ws / plain_step_qps, "queries": qps / ws / plain_qps,
+                                  "train": tps / ws / plain_tps},
         "final_stats": {"mean_loss": ours["loss"][0], "grad_norm": ours["loss"][1]},
         "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s (query + train step, host buffers)",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
@@ -509,10 +523,15 @@ def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
     O.adam_ema(gr, 128.0, 1e-2, 0.9, 0.99, 1e-15, 1e-6, 0.95, 1, w, mm, vv, ps, ema, net.n_mlp_params)
     ta = time.perf_counter() - ta
     per_sample = tt / tdone + ta / N_TRAIN
-    return {"value": done / tq, "unit": "queries/s", "train_samples_per_s": 1.0 / per_sample,
+    # one step of the workload: a query pass over N_QUERIES and a training step of N_TRAIN samples
+    t_step = N_QUERIES * tq / done + N_TRAIN * per_sample
+    return {"value": N_QUERIES / t_step, "unit": "queries/s (query pass + training step)",
+            "train_samples_per_s": N_TRAIN / t_step, "query_pass_queries_per_s": done / tq,
+            "train_step_samples_per_s": 1.0 / per_sample,
             "cores": O.num_threads(), "kind": kind,
             "sample": "%d queries and %d training samples of the same workload (FP32 reference-order mixture, "
-                      "FP64 restated encoding+MLP, OpenMP)" % (done, tdone)}
+                      "FP64 restated encoding+MLP, OpenMP), scaled to one step of 2,073,600 queries and "
+                      "262,144 training samples" % (done, tdone)}
 
 
 def run_reference(args):
@@ -529,11 +548,12 @@ def run_reference(args):
     for _ in range(args.warmup):
         cpu_baseline(q, x, rec, seconds=1.0)
     t0 = time.perf_counter()
-    vals, tvals, last = [], [], None
+    vals, tvals, qvals, last = [], [], [], None
     for _ in range(args.steps):
         last = cpu_baseline(q, x, rec, seconds=per)
         vals.append(last["value"])
         tvals.append(last["train_samples_per_s"])
+        qvals.append(last["query_pass_queries_per_s"])
     wall = time.perf_counter() - t0
     v = float(np.mean(vals))
     line = {
@@ -545,6 +565,9 @@ def run_reference(args):
         "config": {"workload": "full guiding step: 2,073,600-query wavefront (1920x1080) + 2^18-sample train step",
                    "sample": "bounded per step; throughput scaled to the unit"},
         "train_samples_per_s": float(np.mean(tvals)),
+        "rates": "value and train_samples_per_s: a step's 2,073,600 queries and 2^18 training samples over the "
+                 "step's time (query pass + training step); query_pass: the query phase alone",
+        "query_pass": {"queries_per_s": float(np.mean(qvals))},
         "cpu_baseline": {"value": v, "unit": "queries/s", "cores": last["cores"], "kind": "port",
                          "sample": last["sample"]},
         "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
