@@ -443,6 +443,20 @@ nmg_status nmg_autotune_query(nmg_ctx* ctx, const nmg_shading* in, const float* 
  * gave up). */
 nmg_status nmg_check_errors(nmg_ctx* ctx);
 
+/*
+ * Failure-detection self-test (no counterpart in the reference, which exits
+ * through Log(Fatal) instead of reporting device-side failures). Launches,
+ * on `stream`, one thread that waits through the same bounded device wait
+ * the fused kernels use on a barrier nothing arrives at: after about 2e9 SM
+ * cycles (about one second at the maximum clock) the wait gives up, the
+ * kernel records a timeout in the context's device error flag and returns.
+ * The next nmg_check_errors then returns NMG_ERR_TIMEOUT and clears the
+ * flag; the context stays usable. NMG_ERR_UNSUPPORTED for a context without
+ * fused kernel state: the plain FP32 path (it has no device waits), or a
+ * 16-bit configuration before its first nmg_reserve.
+ */
+nmg_status nmg_selftest_wait_timeout(nmg_ctx* ctx, nmg_stream stream);
+
 /* Host-file checkpoint of {master params, inference params, Adam moments,
  * step counters, step}. */
 nmg_status nmg_save(const nmg_ctx* ctx, const char* path);

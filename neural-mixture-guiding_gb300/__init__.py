@@ -204,6 +204,7 @@ def _bind_field(L):
         "nmg_set_query_tiling": [P, C.c_int],
         "nmg_autotune_query": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), C.c_int, C.POINTER(C.c_int), P],
         "nmg_check_errors": [P],
+        "nmg_selftest_wait_timeout": [P, P],
         "nmg_save": [P, C.c_char_p],
         "nmg_export_tcnn": [P, C.c_char_p, C.c_int],
         "nmg_extract_records": [P, C.POINTER(RadianceRecords), C.POINTER(TrainPixels), C.c_int, P, P, P, P],
@@ -443,6 +444,11 @@ class GuidingField:
 
     def check_errors(self):
         check(self.L.nmg_check_errors(self.h))
+
+    def selftest_wait_timeout(self, stream=None):
+        """Runs a kernel whose bounded device wait gives up (about a second); the next
+        check_errors() raises NMGError with NMG_ERR_TIMEOUT."""
+        check(self.L.nmg_selftest_wait_timeout(self.h, _stream(stream)))
 
     def extract_records(self, records, cur_depth, offset, stride, train_res, res, capacity, product=True,
                         stream=None):

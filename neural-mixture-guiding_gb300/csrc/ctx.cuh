@@ -96,6 +96,7 @@ nmg_status fused_pdf(nmg_ctx* c, const nmg_shading* in, const float* wi, const i
 nmg_status pack_images(nmg_ctx* c, cudaStream_t st);
 void fused_release(nmg_ctx* c);
 nmg_status fused_check_errors(nmg_ctx* c);
+nmg_status fused_selftest_wait_timeout(nmg_ctx* c, cudaStream_t st);
 nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, int n, const nmg_query_out* out,
                           int use_cache, int* chosen, cudaStream_t st);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,

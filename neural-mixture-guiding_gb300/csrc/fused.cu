@@ -386,6 +386,30 @@ nmg_status fused_infer_raw(nmg_ctx* c, const float* x, const int* d_count, int n
   return dispatch_query(c, a, st);
 }
 
+// Failure-detection self-test: one thread waits, through the same bounded
+// mbarrier wait every fused kernel uses (tc::mbar_wait, about 2e9 SM cycles),
+// on a barrier that nothing arrives at. The wait gives up, the kernel records
+// code 9 in the context's device error flag, as a fused kernel does when one
+// of its waits gives up, and returns; nothing else runs in it.
+constexpr int kSelftestTimeoutCode = 9;
+__global__ void k_selftest_wait_timeout(int* err) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+    if (!tc::mbar_wait(&bar, 0)) atomicExch(err, kSelftestTimeoutCode);
+  }
+}
+
+nmg_status fused_selftest_wait_timeout(nmg_ctx* c, cudaStream_t st) {
+  FusedState* s = fstate(c);
+  if (!s)
+    return set_error(NMG_ERR_UNSUPPORTED,
+                     "no fused kernel state (an FP32 configuration, or nmg_reserve not called): no device error flag");
+  k_selftest_wait_timeout<<<1, 32, 0, st>>>(s->err);
+  return check_launch("k_selftest_wait_timeout");
+}
+
 nmg_status fused_check_errors(nmg_ctx* c) {
   FusedState* s = fstate(c);
   if (!s) return NMG_OK;

@@ -496,6 +496,11 @@ nmg_status nmg_check_errors(nmg_ctx* c) {
   return fused_check_errors(c);
 }
 
+nmg_status nmg_selftest_wait_timeout(nmg_ctx* c, nmg_stream stream) {
+  NMG_REQUIRE(c != nullptr, "ctx is NULL");
+  return fused_selftest_wait_timeout(c, (cudaStream_t)stream);
+}
+
 static const uint32_t kMagic = 0x31474d4e;  // "NMG1"
 
 nmg_status nmg_save(const nmg_ctx* c, const char* path) {
