@@ -220,6 +220,7 @@ def run_ours(args):
     plain = measure(nmg.PATH_FP32, max(1, min(args.steps, 3)), 1) if path != nmg.PATH_FP32 else ours
     frame = frame_graph(nmg, synth, torch, np, dx, drec, path) if path != nmg.PATH_FP32 and not args.no_frame else None
     mix = mixture_kernels(nmg, synth, torch, flush, peaks()[0])
+    nxt = next_rows(nmg, torch, ours["field"], dq, ours["out"]["dir"], flush) if path != nmg.PATH_FP32 else None
 
     # end to end through the public API on host buffers (nmg_query_host / nmg_train_step_host): pinned host
     # inputs in, host results out, every step; the library pipelines the copies with the kernels
@@ -331,6 +332,7 @@ def run_ours(args):
         "clocks": ours["clocks"],
         "frame_graph": frame,
         "mixture_kernels": mix,
+        "next_rows": nxt,
     }
     line["gpu_launches"] = launches_per_step(path) * steps
     print(json.dumps(line), flush=True)
@@ -465,6 +467,60 @@ def mixture_kernels(nmg, synth, torch, flush, hbm, n=1 << 21, K=8, reps=10):
         gbs = per * n / t / 1e9
         out[name] = {"us": t * 1e6, "bytes_per_query": per, "achieved_gbs": gbs, "hbm_frac": gbs / hbm}
     return out
+
+
+def next_rows(nmg, torch, f, dq, dirs, flush, reps=5, depth=6):
+    """The calls built around the guiding step, timed through the C ABI with CUDA events (L2 flushed before
+    each launch, median of `reps`):
+      * the MIS pdf at given directions over the 1920x1080 wavefront (nmg_pdf: featurise, encode, MLP and
+        the mixture pdf in one fused pass, no raw outputs through HBM);
+      * training-record extraction from the per-pixel radiance records of a 1920x1080 frame with `depth`
+        bounces per pixel, every pixel a training pixel (nmg_extract_records; the call also resets its
+        4-byte append counter). Records: seeded uniform values, bounce counts uniform in 0..depth."""
+    st = torch.cuda.current_stream()
+
+    def timed(fn):
+        for _ in range(3):
+            fn()
+        ts = []
+        for i in range(reps):
+            flush(i)
+            a, b = torch.cuda.Event(True), torch.cuda.Event(True)
+            a.record(st)
+            fn()
+            b.record(st)
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / 1e3)
+        return sorted(ts)[reps // 2]
+
+    t_pdf = timed(lambda: f.pdf(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dirs))
+    res = (1920, 1080)
+    n = res[0] * res[1]
+    g = torch.Generator(device="cuda").manual_seed(11)
+
+    def u(*shape, lo=0.0, hi=1.0):
+        return torch.rand(*shape, device="cuda", generator=g) * (hi - lo) + lo
+
+    def angles():
+        return torch.stack([u(n, hi=math.pi), u(n, hi=2 * math.pi)], 1).contiguous()
+
+    recs = [{"L": u(n, 3), "thp": u(n, 3), "pos": u(n, 3), "dir": angles(), "wi_pdf": u(n, lo=0.01, hi=2.0),
+             "bsdf_pdf": u(n, lo=0.01, hi=2.0), "mis_weight": u(n), "delta": (u(n) < 0.1).to(torch.uint8),
+             "bsdf_val": u(n, 3), "wo": angles(), "normal": angles(), "roughness": u(n)} for _ in range(depth)]
+    cur = torch.randint(0, depth + 1, (n,), device="cuda", dtype=torch.int32, generator=g)
+    cap = n * depth
+    outs = (torch.empty((cap, int(f.info.n_input)), device="cuda"),
+            torch.empty((cap, int(f.info.record_floats)), device="cuda"),
+            torch.zeros(1, dtype=torch.int32, device="cuda"))
+
+    def extract():
+        f.extract_records(recs, cur, (0, 0), (1, 1), res, res, cap, outputs=outs)
+
+    t_ex = timed(extract)
+    n_rec = int(outs[2].item())
+    return {"mis_pdf": {"queries": N_QUERIES, "us": t_pdf * 1e6, "queries_per_s": N_QUERIES / t_pdf},
+            "record_extraction": {"pixels": n, "bounces_per_pixel": depth, "records": n_rec, "us": t_ex * 1e6,
+                                  "pixels_per_s": n / t_ex, "records_per_s": n_rec / t_ex}}
 
 
 def launches_per_step(path):

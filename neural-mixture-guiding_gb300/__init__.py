@@ -451,10 +451,11 @@ class GuidingField:
         check(self.L.nmg_selftest_wait_timeout(self.h, _stream(stream)))
 
     def extract_records(self, records, cur_depth, offset, stride, train_res, res, capacity, product=True,
-                        stream=None):
+                        stream=None, outputs=None):
         """nmg_extract_records: records = list (one per depth) of dicts of device tensors (L, thp, pos, dir,
         wi_pdf, bsdf_pdf, mis_weight, delta (uint8), bsdf_val, wo, normal, roughness). Returns
-        (x [capacity, n_input], records [capacity, record_floats], count (device int32 [1]))."""
+        (x [capacity, n_input], records [capacity, record_floats], count (device int32 [1])); `outputs`
+        = such a triple to write into instead."""
         import torch
         r = RadianceRecords()
         r.max_depth = len(records)
@@ -466,9 +467,12 @@ class GuidingField:
                 setattr(r.depth[d], name, t.data_ptr() if t is not None else None)
         tp = TrainPixels((C.c_uint * 2)(*offset), (C.c_uint * 2)(*stride), (C.c_uint * 2)(*train_res),
                          (C.c_uint * 2)(*res))
-        x = torch.zeros((capacity, self.info.n_input), device="cuda")
-        rec = torch.zeros((capacity, self.info.record_floats), device="cuda")
-        cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+        if outputs is not None:
+            x, rec, cnt = outputs  # nmg_extract_records resets the count itself
+        else:
+            x = torch.zeros((capacity, self.info.n_input), device="cuda")
+            rec = torch.zeros((capacity, self.info.record_floats), device="cuda")
+            cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
         check(self.L.nmg_extract_records(self.h, C.byref(r), C.byref(tp), int(capacity), _ptr(x), _ptr(rec),
                                          _ptr(cnt), _stream(stream)))
         return x, rec, cnt
