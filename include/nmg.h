@@ -357,8 +357,10 @@ int nmg_get_query_tiling(const nmg_ctx* ctx);
  * workqueue.h:26-67). For every training pixel (offset + stride * (i, j) over
  * train_res, clipped to res) and every recorded non-delta vertex, appends one
  * network input row x[..][n_input] and one record[..][record_floats]
- * {theta, phi, L / thp * misWeight [* bsdfVal], wiPdf[, bsdfPdf]}; vertices
- * with NaN position, direction, pdf or radiance or a zero pdf are dropped.
+ * {theta, phi, L / thp * misWeight [* bsdfVal], wiPdf[, bsdfPdf]}. As in
+ * train.cu:57-62, a vertex is dropped when its normalised position, its
+ * direction, its warped outgoing direction, its pdf or L / thp * misWeight
+ * (before the bsdfVal factor) has a NaN, or its pdf is zero.
  * *d_count (device) receives the number of records, which can be passed to
  * nmg_train_step as its device count; rows beyond `capacity` are counted but
  * not written. Record order is not deterministic (atomic append, as the

@@ -158,6 +158,22 @@ NMG_D void encode_directional(const EncodingParams& e, const float* x, float* ou
   for (int k = e.levels * e.feats + o; k < e.n_enc_pad; ++k) out[o++] = 1.f;
 }
 
+// normalizeSpatialCoord (train.h:173-177) one IEEE operation at a time in the
+// reference's order, without contraction into fused multiply-adds, so that the
+// result equals the reference's FP32 value bit for bit: the box is inflated by
+// 0.005 x its diagonal's length (Eigen sums the squares as x^2 + (y^2 + z^2)),
+// then 0.5 + (p - centre) / diagonal per axis.
+NMG_D float aabb_inflation(const float* aabb) {
+  const float dx = __fsub_rn(aabb[3], aabb[0]), dy = __fsub_rn(aabb[4], aabb[1]), dz = __fsub_rn(aabb[5], aabb[2]);
+  const float n2 = __fadd_rn(__fmul_rn(dx, dx), __fadd_rn(__fmul_rn(dy, dy), __fmul_rn(dz, dz)));
+  return __fmul_rn(__fsqrt_rn(n2), 0.005f);
+}
+NMG_D float normalize_coord(const float* aabb, float infl, int k, float p) {
+  const float lo = __fsub_rn(aabb[k], infl), hi = __fadd_rn(aabb[k + 3], infl);
+  const float ctr = __fdiv_rn(__fadd_rn(lo, hi), 2.f);
+  return __fadd_rn(0.5f, __fdiv_rn(__fsub_rn(p, ctr), __fsub_rn(hi, lo)));
+}
+
 // train.cu:174-191 (mode 0) / SH-of-normal variant (mode 1): shading data ->
 // network input row x[n_input]. The box is inflated by 0.5% of its diagonal
 // (train.h:173-177).
@@ -171,13 +187,9 @@ NMG_D void featurize(const EncodingParams& e, f3 pos, f3 wo, f3 n, float rough, 
 #pragma unroll
     for (int d = 0; d < 3; ++d) x[d] = 0.5f + (p[d] - e.center[d]) * e.inv_size[d];
   } else {
-    f3 dg{e.aabb[3] - e.aabb[0], e.aabb[4] - e.aabb[1], e.aabb[5] - e.aabb[2]};
-    float infl = sqrtf(dot3(dg, dg)) * 0.005f;
+    const float infl = aabb_inflation(e.aabb);
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      float lo = e.aabb[d] - infl, hi = e.aabb[d + 3] + infl;
-      x[d] = 0.5f + (p[d] - (lo + hi) / 2.f) / (hi - lo);
-    }
+    for (int d = 0; d < 3; ++d) x[d] = normalize_coord(e.aabb, infl, d, p[d]);
   }
   f3 w = FAST ? unit3f(wo) : normalize3(wo);
   x[3] = (w.x + 1.f) * 0.5f;

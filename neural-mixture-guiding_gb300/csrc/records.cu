@@ -9,8 +9,12 @@
 // GuidedOutput pair: the local incident radiance L / thp (channels with
 // thp > 1e-5) weighted by the MIS weight (and by the BSDF value with product
 // sampling), its direction and pdfs, and the network inputs of the vertex.
-// Records with NaN position, direction, pdf or radiance, or a zero pdf, are
-// dropped. Here one thread per training pixel walks its vertices and appends
+// A record is dropped, as in train.cu:57-62, when its normalised position,
+// its direction, its warped outgoing direction, its pdf or its local radiance
+// (tested BEFORE the BSDF factor, which multiplies only the stored copy) has
+// a NaN, or its pdf is zero; a NaN BSDF value alone keeps the record, with a
+// NaN radiance, as it does in the reference. Here one thread per training
+// pixel walks its vertices and appends
 // the records with one atomic per block and vertex depth (block-aggregated:
 // the append counter is a single address, and one atomic per warp and depth
 // serialised on it: 715 -> 530 us for a 1920x1080 frame of 6 bounces), so the
@@ -66,15 +70,18 @@ __global__ void __launch_bounds__(kRecordThreads) k_extract_records(const __grid
           const float th = R.dir[2 * pixel], ph = R.dir[2 * pixel + 1];
           const float wi_pdf = R.wi_pdf[pixel];
           const float mis = R.mis_weight[pixel];
-          float L[3];
+          // local radiance (train.cu:44-49): L / thp per channel with thp > 1e-5,
+          // times the MIS weight. The NaN test below reads this L; the BSDF value
+          // multiplies only the stored copy (train.cu:50-53), as in the reference.
+          float L[3], Lout[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
             const float thp = R.thp[3 * pixel + c];
-            L[c] = thp > NMG_EPS ? R.L[3 * pixel + c] / thp : 0.f;
-            L[c] *= mis;
-            if (a.r.product && R.bsdf_val) L[c] *= R.bsdf_val[3 * pixel + c];
+            L[c] = thp > NMG_EPS ? __fdiv_rn(R.L[3 * pixel + c], thp) : 0.f;
+            L[c] = __fmul_rn(L[c], mis);
+            Lout[c] = (a.r.product && R.bsdf_val) ? __fmul_rn(L[c], R.bsdf_val[3 * pixel + c]) : L[c];
           }
-          // network inputs (train.cu:30-40): the position in the inflated box,
+          // network inputs (train.cu:34-43): the position in the inflated box,
           // the outgoing direction and the auxiliary normal/roughness inputs
           float sw, cw, sp, cp;
           sincosf(R.wo[2 * pixel], &sw, &cw);
@@ -82,14 +89,10 @@ __global__ void __launch_bounds__(kRecordThreads) k_extract_records(const __grid
           const f3 wo{sw * cp, sw * sp, cw};
           const float nth = R.normal[2 * pixel], nph = R.normal[2 * pixel + 1];
           const float rough = R.roughness[pixel];
-          // normalizeSpatialCoord (train.h:173-177), the same expressions as featurize()
+          // normalizeSpatialCoord (train.h:173-177), bit for bit
           const float p[3] = {pos.x, pos.y, pos.z};
-          const f3 dg{a.enc.aabb[3] - a.enc.aabb[0], a.enc.aabb[4] - a.enc.aabb[1], a.enc.aabb[5] - a.enc.aabb[2]};
-          const float infl = sqrtf(dot3(dg, dg)) * 0.005f;
-          for (int k = 0; k < 3; ++k) {
-            const float lo = a.enc.aabb[k] - infl, hi = a.enc.aabb[k + 3] + infl;
-            xin[k] = 0.5f + (p[k] - (lo + hi) / 2.f) / (hi - lo);
-          }
+          const float infl = aabb_inflation(a.enc.aabb);
+          for (int k = 0; k < 3; ++k) xin[k] = normalize_coord(a.enc.aabb, infl, k, p[k]);
           xin[3] = (wo.x + 1.f) * 0.5f;
           xin[4] = (wo.y + 1.f) * 0.5f;
           xin[5] = (wo.z + 1.f) * 0.5f;
@@ -108,14 +111,18 @@ __global__ void __launch_bounds__(kRecordThreads) k_extract_records(const __grid
           }
           out[0] = th;
           out[1] = ph;
-          out[2] = L[0];
-          out[3] = L[1];
-          out[4] = L[2];
+          out[2] = Lout[0];
+          out[3] = Lout[1];
+          out[4] = Lout[2];
           out[5] = wi_pdf;
           out[6] = R.bsdf_pdf ? R.bsdf_pdf[pixel] : 0.f;
-          // train.cu:60-65
-          keep = !(isnan(pos.x) || isnan(pos.y) || isnan(pos.z) || isnan(th) || isnan(ph) || isnan(wi_pdf) ||
-                   wi_pdf == 0.f || isnan(L[0]) || isnan(L[1]) || isnan(L[2]));
+          // train.cu:57-62: NaN in the normalised position, the stored direction,
+          // the warped outgoing direction (the networks here always take wo as an
+          // input, as the reference's default product-sampling build does), the
+          // pdf or the local radiance before the BSDF factor, or a zero pdf
+          keep = !(isnan(xin[0]) || isnan(xin[1]) || isnan(xin[2]) || isnan(th) || isnan(ph) || isnan(xin[3]) ||
+                   isnan(xin[4]) || isnan(xin[5]) || isnan(wi_pdf) || wi_pdf == 0.f || isnan(L[0]) ||
+                   isnan(L[1]) || isnan(L[2]));
         }
       }
       // block-aggregated append: the warps' counts, one atomic for the block, then each warp's offset

@@ -181,7 +181,11 @@ def ref_lib():
         P = C.c_void_p
         L.ref_mixture_sample.argtypes = [P, C.c_int, C.c_long, P, P, P, P, P]
         L.ref_mixture_pdf.argtypes = [P, C.c_int, C.c_long, P, P, P]
-        L.ref_loss_grad.argtypes = [P, C.c_int, C.c_long, P, C.c_float, P, P]
+        L.ref_dL_doutput_divergence.argtypes = [P, C.c_int, C.c_long, P, C.c_float, P, P]
+        L.ref_generate_training_data.argtypes = [P] * 12 + [P, C.c_int, C.c_int] + [P] * 5 + [C.c_int, P, P]
+        L.ref_generate_training_data.restype = C.c_int
+        L.ref_generate_inference_data.argtypes = [P, P, P, P, C.c_int, P, P, P, P, P, P]
+        L.ref_generate_inference_data.restype = C.c_int
         _ref = L
     return _ref
 
@@ -205,62 +209,127 @@ def ref_mixture_pdf(raw, wi, cos_normal=None):
 
 
 def ref_loss_grad(raw, samples, loss_scale=128.0):
+    """The reference's compute_dL_doutput_divergence kernel (train.cu:69-124) run on the host: __half raw
+    outputs and gradients, per-sample likelihood."""
     raw, samples = _f32(raw), _f32(samples)
     n = raw.shape[0]
     g = np.zeros(raw.shape, np.float32)
     loss = np.zeros(n, np.float32)
-    ref_lib().ref_loss_grad(_p(raw), raw.shape[1], n, _p(samples), float(loss_scale), _p(g), _p(loss))
+    ref_lib().ref_dL_doutput_divergence(_p(raw), raw.shape[1], n, _p(samples), float(loss_scale), _p(g), _p(loss))
     return g, loss
+
+
+def ref_extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, capacity=None):
+    """The reference's generate_training_data kernel (train.cu:14-67) run on the host over a
+    GuidedPixelStateBuffer built from the per-depth arrays of `rec` (as extract_records takes them; every
+    depth of the reference's MAX_TRAIN_DEPTH = 8 must be present). Returns (x [n, 9], records [n, 6]) in
+    the reference's push order."""
+    D = len(rec["L"])
+    npx = int(np.asarray(cur_depth).size)
+
+    def stack(k, w, dt=np.float32):
+        return np.ascontiguousarray(np.stack([np.asarray(rec[k][d], dt).reshape(npx, w) for d in range(D)]))
+
+    arrs = [stack("L", 3), stack("thp", 3), stack("pos", 3), stack("dir", 2), stack("wi_pdf", 1),
+            stack("bsdf_pdf", 1), stack("mis_weight", 1), stack("delta", 1, np.uint8), stack("bsdf_val", 3),
+            stack("wo", 2), stack("normal", 2), stack("roughness", 1)]
+    cur = np.ascontiguousarray(np.asarray(cur_depth, np.uint32))
+    u = [np.ascontiguousarray(np.asarray(v, np.uint32)) for v in (offset, stride, train_res, res)]
+    box = _f32(np.asarray(aabb, np.float32))
+    cap = int(capacity if capacity is not None else npx * D)
+    L = ref_lib()
+    ni, no = 9, 6
+    x = np.zeros((cap, ni), np.float32)
+    out = np.zeros((cap, no), np.float32)
+    n = L.ref_generate_training_data(*[_p(a) for a in arrs], _p(cur), npx, D, *[_p(a) for a in u], _p(box), cap,
+                                     _p(x), _p(out))
+    n = min(n, cap)
+    return x[:n], out[:n]
+
+
+def ref_featurize_queue(pos, wo, normal, rough, aabb):
+    """The reference's generate_inference_data kernel (train.cu:174-191) run on the host over a
+    ScatterRayQueue (its soac-generated SOA<ScatterRayWorkItem>) filled with the given shading data.
+    Returns (x [n, 9], leaves) where leaves holds the queue's own field arrays sd.pos / sd.wo / sd.frame.N
+    ([n, 3]) and sd.roughness ([n]) as the SOA stores them."""
+    pos, wo, normal, rough = (_f32(np.asarray(a, np.float32)) for a in (pos, wo, normal, rough))
+    n = pos.shape[0]
+    box = _f32(np.asarray(aabb, np.float32))
+    x = np.zeros((n, 9), np.float32)
+    lv = {k: np.zeros((n, 3), np.float32) for k in ("pos", "wo", "normal")}
+    lv["roughness"] = np.zeros(n, np.float32)
+    ni = ref_lib().ref_generate_inference_data(_p(pos), _p(wo), _p(normal), _p(rough), n, _p(box), _p(x),
+                                               _p(lv["pos"]), _p(lv["wo"]), _p(lv["normal"]), _p(lv["roughness"]))
+    assert ni == 9
+    return x, lv
 
 
 def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_mode=0, product=True,
                     selection=False):
     """Training records from per-pixel radiance records, restating the
     reference's generate_training_data (src/render/guided/train.cu:14-67) with
-    normalizeSpatialCoord (train.h:173-177) in FP64 numpy.
+    normalizeSpatialCoord (train.h:173-177) in FP32, one IEEE operation at a
+    time in the reference's order (numpy float32 scalars round every step), so
+    the kept-record set, the positions and the radiance values are exact.
+
+    Filter (train.cu:57-62): a vertex is dropped when the normalised position,
+    the stored direction, the warped outgoing direction (product sampling, the
+    reference's default, train.cu:36-37), the pdf or the local radiance
+    L / thp * misWeight has a NaN, or the pdf is zero. The radiance is tested
+    BEFORE the bsdfVal product (train.cu:50-53 multiply only output.L), so a
+    NaN bsdfVal keeps the record with a NaN radiance.
 
     rec: dict of per-depth arrays [depth][pixels(, c)]: L, thp, pos, bsdf_val
     (3 channels), dir, wo, normal (2 angles), wi_pdf, bsdf_pdf, mis_weight,
-    roughness, delta. Returns (x [n, 9|10], records [n, 6|7]) in the
-    reference's loop order (training pixel, then depth)."""
-    aabb = np.asarray(aabb, np.float64)
+    roughness, delta. Returns (x [n, 9|10], records [n, 6|7]) as float32 in
+    the reference's loop order (training pixel, then depth)."""
+    f = np.float32
+    aabb = np.asarray(aabb, np.float32)
     mn, mx = aabb[:3], aabb[3:]
-    infl = np.linalg.norm(mx - mn) * 0.005  # AABB::inflate by diagonal * 0.005
+    dg = mx - mn
+    # AABB::inflate(diagonal().norm() * 0.005f): Eigen's unrolled sum is x^2 + (y^2 + z^2)
+    infl = f(np.sqrt(f(dg[0] * dg[0]) + f(f(dg[1] * dg[1]) + f(dg[2] * dg[2])))) * f(0.005)
     lo, hi = mn - infl, mx + infl
+    ctr = (lo + hi) / f(2)
+    diag = hi - lo
+    eps = f(1e-5)  # M_EPSILON (krrmath constants.h:25)
     xs, outs = [], []
-    for ty in range(train_res[1]):
-        for tx in range(train_res[0]):
-            px, py = tx * stride[0] + offset[0], ty * stride[1] + offset[1]
-            if px >= res[0] or py >= res[1]:
-                continue
-            pid = px + py * res[0]
-            for d in range(min(int(cur_depth[pid]), len(rec["L"]))):
-                if rec["delta"][d][pid]:
+    with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
+        for ty in range(train_res[1]):
+            for tx in range(train_res[0]):
+                px, py = tx * stride[0] + offset[0], ty * stride[1] + offset[1]
+                if px >= res[0] or py >= res[1]:
                     continue
-                pos = rec["pos"][d][pid].astype(np.float64)
-                p = 0.5 + (pos - (lo + hi) / 2) / (hi - lo)
-                th, ph = rec["wo"][d][pid].astype(np.float64)
-                wo = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)])
-                nt, npf = rec["normal"][d][pid].astype(np.float64)
-                r = float(rec["roughness"][d][pid])
-                if input_mode == 0:
-                    aux = [nt / np.pi, npf / (2 * np.pi), 1 - np.exp(-r)]
-                else:
-                    n3 = np.array([np.sin(nt) * np.cos(npf), np.sin(nt) * np.sin(npf), np.cos(nt)])
-                    aux = list((n3 + 1) / 2) + [1 - np.exp(-r)]
-                thp = rec["thp"][d][pid].astype(np.float64)
-                L = np.where(thp > 1e-5, rec["L"][d][pid].astype(np.float64) / np.where(thp > 1e-5, thp, 1), 0.0)
-                L = L * float(rec["mis_weight"][d][pid])
-                if product:
-                    L = L * rec["bsdf_val"][d][pid].astype(np.float64)
-                direc = rec["dir"][d][pid].astype(np.float64)
-                wi_pdf = float(rec["wi_pdf"][d][pid])
-                if np.isnan(pos).any() or np.isnan(direc).any() or np.isnan(wi_pdf) or wi_pdf == 0 or np.isnan(L).any():
-                    continue
-                xs.append(np.concatenate([p, (wo + 1) / 2, aux]))
-                o = [direc[0], direc[1], L[0], L[1], L[2], wi_pdf]
-                if selection:
-                    o.append(float(rec["bsdf_pdf"][d][pid]))
-                outs.append(o)
+                pid = px + py * res[0]
+                for d in range(min(int(cur_depth[pid]), len(rec["L"]))):
+                    if rec["delta"][d][pid]:
+                        continue
+                    pos = rec["pos"][d][pid].astype(np.float32)
+                    p = f(0.5) + (pos - ctr) / diag
+                    th, ph = (f(v) for v in rec["wo"][d][pid])
+                    wo = np.array([np.sin(th) * np.cos(ph), np.sin(th) * np.sin(ph), np.cos(th)], np.float32)
+                    wdir = (wo + f(1)) * f(0.5)
+                    nt, npf = (f(v) for v in rec["normal"][d][pid])
+                    r = f(rec["roughness"][d][pid])
+                    if input_mode == 0:
+                        aux = [nt * f(1 / np.pi), npf * f(1 / (2 * np.pi)), f(1) - np.exp(-r)]
+                    else:
+                        n3 = np.array([np.sin(nt) * np.cos(npf), np.sin(nt) * np.sin(npf), np.cos(nt)], np.float32)
+                        aux = list((n3 + f(1)) * f(0.5)) + [f(1) - np.exp(-r)]
+                    thp = rec["thp"][d][pid].astype(np.float32)
+                    Lr = rec["L"][d][pid].astype(np.float32)
+                    L = np.array([Lr[c] / thp[c] if thp[c] > eps else f(0) for c in range(3)], np.float32)
+                    L = L * f(rec["mis_weight"][d][pid])
+                    Lout = L * rec["bsdf_val"][d][pid].astype(np.float32) if product else L
+                    direc = rec["dir"][d][pid].astype(np.float32)
+                    wi_pdf = f(rec["wi_pdf"][d][pid])
+                    if (np.isnan(p).any() or np.isnan(direc).any() or np.isnan(wdir).any() or np.isnan(wi_pdf)
+                            or wi_pdf == 0 or np.isnan(L).any()):
+                        continue
+                    xs.append(np.concatenate([p, wdir, np.array(aux, np.float32)]))
+                    o = [direc[0], direc[1], Lout[0], Lout[1], Lout[2], wi_pdf]
+                    if selection:
+                        o.append(f(rec["bsdf_pdf"][d][pid]))
+                    outs.append(o)
     ni = 9 if input_mode == 0 else 10
-    return (np.array(xs, np.float64).reshape(-1, ni), np.array(outs, np.float64).reshape(-1, 7 if selection else 6))
+    return (np.array(xs, np.float32).reshape(-1, ni), np.array(outs, np.float32).reshape(-1, 7 if selection else 6))

@@ -12,8 +12,11 @@ Outputs come from the reference's distribution.h / vmf.h / train.h compiled
 on the host (K = 8, the reference's compile-time lobe count):
   sample  -- MixedSG(raw).sample() + pdf(), with and without applyCosineLobe
   pdf     -- MixedSG(raw).pdf(wi) at given directions
-  loss    -- the per-sample body of compute_dL_doutput_divergence
-             (train.cu:80-123) with __half raw outputs and gradients.
+  loss    -- the reference's compute_dL_doutput_divergence kernel
+             (train.cu:69-124) run on the host, with __half raw outputs and
+             gradients.
+It also writes tests/golden/train_cu_golden.npz from the reference's
+generate_training_data and generate_inference_data kernels (train_cu()).
 """
 import importlib
 import os
@@ -97,5 +100,118 @@ def main():
     print("wrote", out, "rows", n, "bytes", os.path.getsize(out))
 
 
+# ---------------------------------------------------------------------------
+# train_cu_golden.npz: the reference's own train.cu kernels (compiled as host
+# functions by oracle/ref_shim.cu) on seeded inputs.
+#   records   -- generate_training_data (train.cu:14-67) over a
+#                GuidedPixelStateBuffer of 8 depths: delta vertices, thp below
+#                and exactly at M_EPSILON = 1e-5, NaN position / direction /
+#                outgoing direction / pdf / MIS weight / radiance, NaN and Inf
+#                bsdfVal, zero pdfs, a training-pixel grid running off the image
+#   featurize -- generate_inference_data (train.cu:174-191) over a
+#                ScatterRayQueue (soac-generated SOA<ScatterRayWorkItem>):
+#                positions inside, on and outside the box, non-unit outgoing
+#                directions, normals on the axes and poles; the queue's own
+#                field arrays are stored with the rows
+# ---------------------------------------------------------------------------
+REC_RES = (29, 23)
+REC_OFFSET, REC_STRIDE = (1, 2), (3, 2)
+REC_TRAIN_RES = (10, 12)  # the grid's last row and column fall outside the image
+REC_AABB = (-2.0, -1.5, -2.5, 3.0, 3.5, 2.0)
+DEPTH = 8
+
+
+def record_inputs(seed):
+    rng = np.random.default_rng(seed)
+    n = REC_RES[0] * REC_RES[1]
+    rec = {}
+
+    def ang(m):
+        return np.stack([rng.uniform(0, np.pi, m), rng.uniform(0, 2 * np.pi, m)], 1).astype(np.float32)
+
+    per = []
+    for _ in range(DEPTH):
+        r = {}
+        thp = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+        thp[rng.random((n, 3)) < 0.05] = 5e-6
+        thp[rng.random((n, 3)) < 0.05] = np.float32(1e-5)  # exactly M_EPSILON: not above it
+        r["thp"] = thp
+        L = rng.lognormal(0, 1, (n, 3)).astype(np.float32)
+        L[rng.random(n) < 0.01, 1] = np.nan
+        r["L"] = L
+        pos = rng.uniform(-2.5, 3.5, (n, 3)).astype(np.float32)
+        pos[rng.random(n) < 0.01, 0] = np.nan
+        r["pos"] = pos
+        d = ang(n)
+        d[rng.random(n) < 0.01, 1] = np.nan
+        r["dir"] = d
+        wp = rng.uniform(0.01, 2, n).astype(np.float32)
+        wp[rng.random(n) < 0.02] = 0.0
+        wp[rng.random(n) < 0.01] = np.nan
+        r["wi_pdf"] = wp
+        r["bsdf_pdf"] = rng.uniform(0.01, 2, n).astype(np.float32)
+        mw = rng.uniform(0, 1, n).astype(np.float32)
+        mw[rng.random(n) < 0.01] = np.nan
+        r["mis_weight"] = mw
+        r["delta"] = (rng.random(n) < 0.1).astype(np.uint8)
+        bv = rng.uniform(0, 1, (n, 3)).astype(np.float32)
+        bv[rng.random(n) < 0.02, 0] = np.nan   # kept by the reference: NaN only in the stored radiance
+        bv[rng.random(n) < 0.02, 2] = np.inf
+        r["bsdf_val"] = bv
+        wo = ang(n)
+        wo[rng.random(n) < 0.015, 0] = np.nan  # NaN warped outgoing direction: dropped
+        wo[rng.random(n) < 0.015, 1] = np.nan
+        r["wo"] = wo
+        r["normal"] = ang(n)
+        r["roughness"] = rng.uniform(0, 1, n).astype(np.float32)
+        per.append(r)
+    for k in per[0]:
+        rec[k] = np.stack([r[k] for r in per])
+    cur = rng.integers(0, DEPTH + 1, n).astype(np.uint32)
+    # pixels off the training grid are never read: zero them so the fixture compresses
+    on = np.zeros(n, bool)
+    for ty in range(REC_TRAIN_RES[1]):
+        for tx in range(REC_TRAIN_RES[0]):
+            px, py = tx * REC_STRIDE[0] + REC_OFFSET[0], ty * REC_STRIDE[1] + REC_OFFSET[1]
+            if px < REC_RES[0] and py < REC_RES[1]:
+                on[px + py * REC_RES[0]] = True
+    for k in rec:
+        rec[k][:, ~on] = 0
+    cur[~on] = 0
+    return rec, cur
+
+
+def queue_inputs(seed, n=1024):
+    rng = np.random.default_rng(seed)
+    lo, hi = np.array(REC_AABB[:3], np.float32), np.array(REC_AABB[3:], np.float32)
+    pos = rng.uniform(lo - 0.1, hi + 0.1, (n, 3)).astype(np.float32)
+    pos[:8] = np.array([[x, y, z] for x in (lo[0], hi[0]) for y in (lo[1], hi[1]) for z in (lo[2], hi[2])])
+    wo = synth.uniform_sphere(rng, (n,)).astype(np.float32) * rng.uniform(0.5, 2.0, (n, 1)).astype(np.float32)
+    nrm = synth.uniform_sphere(rng, (n,)).astype(np.float32)
+    axes = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0]], np.float32)
+    nrm[8:14] = axes
+    wo[14:20] = axes * 3.0
+    rough = rng.uniform(0, 1, n).astype(np.float32)
+    rough[20:22] = (0.0, 1.0)
+    return pos, wo, nrm, rough
+
+
+def train_cu():
+    rec, cur = record_inputs(SEED + 11)
+    recd = {k: [v[d] for d in range(DEPTH)] for k, v in rec.items()}
+    x, out = O.ref_extract_records(recd, cur, REC_OFFSET, REC_STRIDE, REC_TRAIN_RES, REC_RES, REC_AABB)
+    pos, wo, nrm, rough = queue_inputs(SEED + 12)
+    fx, leaves = O.ref_featurize_queue(pos, wo, nrm, rough, REC_AABB)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "train_cu_golden.npz")
+    np.savez_compressed(
+        path, res=np.array(REC_RES, np.uint32), offset=np.array(REC_OFFSET, np.uint32),
+        stride=np.array(REC_STRIDE, np.uint32), train_res=np.array(REC_TRAIN_RES, np.uint32),
+        aabb=np.array(REC_AABB, np.float32), cur_depth=cur, **{"rec_" + k: v for k, v in rec.items()},
+        rec_x=x, rec_out=out, q_pos=pos, q_wo=wo, q_normal=nrm, q_rough=rough, q_x=fx,
+        soa_pos=leaves["pos"], soa_wo=leaves["wo"], soa_normal=leaves["normal"], soa_rough=leaves["roughness"])
+    print("wrote", path, "records", len(x), "queries", len(fx), "bytes", os.path.getsize(path))
+
+
 if __name__ == "__main__":
     main()
+    train_cu()
