@@ -50,6 +50,14 @@ TRAFFIC_QUERY_BYTES = 141_388_032 + 37_773_312
 L2_TO_L1_BYTES = 4.679e9
 
 
+# The hash-grid network (NMG_PRESET_HASHGRID) as the oracle describes it; the CPU legs build it from this
+# spec so that the reference arm never loads the product library (tests/test_bench_host.py checks that it
+# equals the library's preset).
+HASHGRID_NET = dict(input_mode=1, grid_hash=1, grid_levels=16, grid_feats=2, grid_log2_T=19, grid_base_res=16,
+                    grid_scale=1.447, grid_smoothstep=0, sh_degree=4, oneblob_bins=4, width=64, n_hidden=3,
+                    n_out=33)
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -160,60 +168,88 @@ def run_ours(args):
     path = {"bf16": nmg.PATH_BF16, "fp16": nmg.PATH_FP16, "fp32": nmg.PATH_FP32}[args.path]
 
     def measure(path_id, steps, warmup, clocks=None):
-        f = nmg.GuidingField(nmg.config(nmg.PRESET_HASHGRID, path=path_id), max_queries=N_QUERIES, max_batch=N_TRAIN)
+        """Times `steps` steps of a freshly created field after `warmup` steps. Every step trains on a
+        fresh batch of records drawn on the GPU from the ground-truth field (as a renderer records new
+        paths each frame), drawn before the step's first event. The clock sampler's warm-up load runs on
+        a separate field, so the timed steps are the field's first steps after its warm-up: the training
+        step is timed on a healthy network (gradient norm reported per step), not on one that hundreds of
+        load steps at the configured learning rate drove into the exp clamp."""
+        cfg = nmg.config(nmg.PRESET_HASHGRID, path=path_id)
+        f = nmg.GuidingField(cfg, max_queries=N_QUERIES, max_batch=N_TRAIN)
+        src = synth.TorchTrainSource(synth.TrainField(seed=replica_seed(rank)), seed=replica_seed(rank) + 3)
         out = {"dir": torch.empty((N_QUERIES, 3), device="cuda"), "pdf": torch.empty(N_QUERIES, device="cuda"),
                "lobe": torch.empty(N_QUERIES, device="cuda", dtype=torch.int32),
                "selection": torch.empty(N_QUERIES, device="cuda")}
-        stats = torch.zeros(2, device="cuda", dtype=torch.float64)
+        stats = torch.zeros((max(steps, 1), 2), device="cuda", dtype=torch.float64)
         st = torch.cuda.current_stream()
         ev = [(torch.cuda.Event(True), torch.cuda.Event(True), torch.cuda.Event(True)) for _ in range(steps)]
         for _ in range(warmup):
+            bx, brec = src(N_TRAIN, selection=True)
             f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
-            f.train_step(dx, drec, stats=stats)
+            f.train_step(bx, brec, stats=stats[0])
         torch.cuda.synchronize()
 
-        def untimed_until(n_samples, limit_s):
-            # keeps the GPU under the same load until the sampler has n_samples clock readings
-            t_end = time.perf_counter() + limit_s
-            while len(clocks.lines) < n_samples and time.perf_counter() < t_end:
-                for _ in range(20):
-                    f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
-                    f.train_step(dx, drec, stats=stats)
-                torch.cuda.synchronize()
-
         if clocks:
-            # clock samples bracket the timed steps: at least two readings under load before them
-            # and two after (the timed region itself is shorter than the sampling interval)
+            # clock samples bracket the timed steps: at least two readings under the same load before
+            # them and two after (the timed region itself is shorter than the sampling interval); the
+            # load runs on a field of its own
+            fl = nmg.GuidingField(cfg, max_queries=N_QUERIES, max_batch=N_TRAIN)
+
+            def untimed_until(n_samples, limit_s):
+                t_end = time.perf_counter() + limit_s
+                while len(clocks.lines) < n_samples and time.perf_counter() < t_end:
+                    for _ in range(20):
+                        fl.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
+                        fl.train_step(dx, drec)
+                    torch.cuda.synchronize()
+
             clocks.start()
             untimed_until(2, 10.0)
             before = len(clocks.lines)
+        batches = [None] * steps
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
         t0 = time.perf_counter()
         for i in range(steps):
+            batches[i] = src(N_TRAIN, selection=True)  # drawn outside the step's events
             flush(i)
             a, b, c = ev[i]
             a.record(st)
             f.query(dq["pos"], dq["wo"], dq["normal"], dq["rough"], dq["u4"], outputs=out)
             b.record(st)
-            f.train_step(dx, drec, stats=stats)
+            f.train_step(batches[i][0], batches[i][1], stats=stats[i])
             c.record(st)
+            batches[i] = None
         torch.cuda.synchronize()
         wall = time.perf_counter() - t0
         if ws > 1:
             torch.distributed.barrier()
         if clocks:
             untimed_until(before + 2, 5.0)
+            fl.close()
         cl = clocks.stop() if clocks else None
         tq = sum(a.elapsed_time(b) for a, b, _ in ev) / 1e3
         tt = sum(b.elapsed_time(c) for _, b, c in ev) / 1e3
-        loss = stats.cpu().numpy().tolist()
-        # one more query with the raw outputs kept, for the kernel-only timing of the query kernel
+        st_np = stats.cpu().numpy()
+        t_steps = [b.elapsed_time(c) for _, b, c in ev]
+        gn = st_np[:steps, 1]
+        healthy = gn >= 1e-3 * gn[0]
+        health = {"grad_norm_first": float(st_np[0, 1]), "grad_norm_last": float(st_np[steps - 1, 1]),
+                  "mean_loss_first": float(st_np[0, 0]), "mean_loss_last": float(st_np[steps - 1, 0]),
+                  "steps_before_first_timed": warmup, "grad_norm_per_step": [float(v) for v in gn],
+                  "train_ms_per_step": [float(v) for v in t_steps],
+                  # the step's work does not depend on the gradient's size: compare the steps whose gradient
+                  # norm is still within 1e-3 of the first timed step's with the rest
+                  "train_ms_healthy_steps": float(np.mean([t for t, h in zip(t_steps, healthy) if h])),
+                  "train_ms_other_steps": float(np.mean([t for t, h in zip(t_steps, healthy) if not h]))
+                  if not healthy.all() else None}
+        if not (health["grad_norm_last"] >= 1e-6 * health["grad_norm_first"] > 0):
+            raise RuntimeError("the network collapsed during the timed steps: %r" % health)
         f.L.nmg_check_errors.argtypes = [ctypes.c_void_p]
         nmg.check(f.L.nmg_check_errors(f.h))
         res = {"t_query": barrier_max(tq, ws), "t_train": barrier_max(tt, ws), "wall": wall, "clocks": cl,
-               "loss": loss, "field": f, "out": out}
+               "loss": st_np[steps - 1].tolist(), "health": health, "field": f, "out": out}
         return res
 
     ours = measure(path, args.steps, args.warmup, Clocks())
@@ -309,11 +345,14 @@ def run_ours(args):
         "plain_fp32": {"step_queries_per_s": plain_step_qps, "query_pass_queries_per_s": plain_qps,
                        "train_step_samples_per_s": plain_tps,
                        "query_ms": plain["t_query"] / p_steps * 1e3, "train_ms": plain["t_train"] / p_steps * 1e3,
-                       "final_stats": {"mean_loss": plain["loss"][0], "grad_norm": plain["loss"][1]}},
+                       "final_stats": {"mean_loss": plain["loss"][0], "grad_norm": plain["loss"][1]},
+                       "train_health": plain["health"]},
         "speedup_vs_plain_fp32": {"step": step_qps / ws / plain_step_qps, "queries": qps / ws / plain_qps,
                                   "train": tps / ws / plain_tps},
         "final_stats": {"mean_loss": ours["loss"][0], "grad_norm": ours["loss"][1]},
-        "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s (query + train step, host buffers)",
+        "train_health": ours["health"],
+        "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s",
+                "what": "query pass + training step per step, host buffers in and out",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                 "api": "nmg_query_host + nmg_train_step_host (pinned host memory)", "final_loss": e2e_loss},
         "gpu_launches": None,
@@ -536,13 +575,14 @@ FUSED_TRAIN_LAUNCHES = 5  # k_fused_train, k_step_inc, k_adam_ema, k_finish_stat
 
 
 def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
-    """The guiding step restated on the host (oracle/, OpenMP), on a bounded sample."""
+    """The guiding step on the host cores (oracle/, OpenMP over every thread), on a bounded sample: the
+    reference-order FP32 mixture code (bit-identical to the reference's own host build) and the FP32
+    restatement of the encodings, MLP and Adam (the reference has no CPU implementation of the network).
+    Builds nothing from the product library."""
     import numpy as np
 
     import oracle as O
-    nmg = importlib.import_module(PKG)
-    cfg = nmg.config(nmg.PRESET_HASHGRID)
-    net = O.make_net(**nmg.oracle_net_spec(cfg))
+    net = O.make_net(**HASHGRID_NET)
     rng = np.random.default_rng(0)
     params = np.zeros(net.n_params, np.float32)
     params[:net.n_mlp_params] = rng.uniform(-0.15, 0.15, net.n_mlp_params)
@@ -554,7 +594,7 @@ def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
     while time.perf_counter() - t0 < seconds / 2 or done == 0:
         sl = slice(done % (N_QUERIES - n), done % (N_QUERIES - n) + n)
         xi = O.featurize(net, q["pos"][sl], q["wo"][sl], q["normal"][sl], q["rough"][sl], q["aabb"])
-        raw = O.network_forward(net, params, xi).astype(np.float32)
+        raw = O.network_forward_f32(net, params, xi)
         s = np.where((q["normal"][sl] * q["wo"][sl]).sum(1, keepdims=True) > 0, 1.0, -1.0).astype(np.float32)
         O.mixture_sample(raw, 8, q["u4"][sl], q["normal"][sl] * s, fp64=False)
         done += n
@@ -565,9 +605,9 @@ def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
     tdone = 0
     while time.perf_counter() - t1 < seconds / 2 or tdone == 0:
         sl = slice(tdone % (N_TRAIN - m), tdone % (N_TRAIN - m) + m)
-        raw = O.network_forward(net, params, x[sl]).astype(np.float32)
+        raw = O.network_forward_f32(net, params, x[sl])
         g, _, _ = O.mixture_loss_grad(raw, 8, rec[sl], 128.0, selection=True, fp64=False)
-        O.network_backward(net, params, x[sl], g)
+        O.network_backward_f32(net, params, x[sl], g)
         tdone += m
     tt = time.perf_counter() - t1
     # Adam over all parameters once per step, timed separately and amortised per sample of a 2^18 batch
@@ -586,8 +626,8 @@ def cpu_baseline(q, x, rec, seconds=15.0, kind="port"):
             "train_step_samples_per_s": 1.0 / per_sample,
             "cores": O.num_threads(), "kind": kind,
             "sample": "%d queries and %d training samples of the same workload (FP32 reference-order mixture, "
-                      "FP64 restated encoding+MLP, OpenMP), scaled to one step of 2,073,600 queries and "
-                      "262,144 training samples" % (done, tdone)}
+                      "FP32 restated encoding + MLP + Adam, OpenMP), scaled to one step of 2,073,600 queries "
+                      "and 262,144 training samples" % (done, tdone)}
 
 
 def run_reference(args):
@@ -626,7 +666,8 @@ def run_reference(args):
         "query_pass": {"queries_per_s": float(np.mean(qvals))},
         "cpu_baseline": {"value": v, "unit": "queries/s", "cores": last["cores"], "kind": "port",
                          "sample": last["sample"]},
-        "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "e2e": {"value": v, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                "what": "query pass + training step per step, on the host cores"},
     }
     print(json.dumps(line), flush=True)
 

@@ -124,7 +124,9 @@ nmg_status nmg_mixture_loss_grad(const nmg_mixture_opts* opts, const float* raw,
  * before any stream capture. All calls share the array: calls that overlap
  * on the GPU (different streams, or different host threads) race on it and
  * must be ordered by the caller. Results equal nmg_mixture_loss_grad's
- * (loss_sum up to the order of the FP64 additions).
+ * (loss_sum up to the order of the FP64 additions). The looked-up address is
+ * kept per device for the life of the process: after a cudaDeviceReset of a
+ * device this entry point must not be called on that device again.
  */
 nmg_status nmg_mixture_loss_grad_noalloc(const nmg_mixture_opts* opts, const float* raw, const float* record,
                                          int record_stride, int n, float loss_scale, float* grad, float* loss,
@@ -342,7 +344,11 @@ nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int 
  * (8: 4 + 2 warpgroups, 4 slots; 9: 5 + 1, 5 slots; 10: 6 + 2, 6 slots;
  * 11: 4 + 2, 8 slots; 12: 4 + 2, 4 slots holding the hidden activations too).
  * 0 selects the default: 12 for the 8-lobe hash-grid network, 8 for the
- * reference network, 4 for 16-lobe networks. nmg_get_query_tiling
+ * reference network, 4 for 16-lobe networks. A tiling whose shared memory
+ * exceeds the device's limit for this network's weight image (11 on the BF16
+ * path, whose query weights carry a second first-layer image) makes the
+ * query calls return NMG_ERR_UNSUPPORTED; the autotuner skips it.
+ * nmg_get_query_tiling
  * reports the tiling in use (0 on the FP32 path). No counterpart in the
  * reference (its FullyFusedMLP launch shape is fixed,
  * fully_fused_mlp.cu:500-558).

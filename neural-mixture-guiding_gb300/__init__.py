@@ -299,6 +299,27 @@ class GuidingField:
     def set_params(self, params):
         check(self.L.nmg_set_params(self.h, _ptr(params), _stream(None)))
 
+    def operand_params(self, which=1):
+        """The parameter values the fused kernels multiply, as FP32 (None on the plain FP32 path):
+        the grid table in the path's 16-bit format; the MLP of the training image (which = 0) all in
+        that format; the MLP of the inference image (which = 1, the query and pdf passes) on the BF16
+        path as bf16(W0) + bf16(W0 - bf16(W0)) for the first layer and FP16 for the later layers, on
+        the FP16 path all FP16."""
+        import torch
+        if self.cfg.path == PATH_FP32:
+            return None
+        p = self.get_params(which)
+        n_mlp = int(self.info.n_mlp_params)
+        if self.cfg.path == PATH_FP16:
+            return p.to(torch.float16).float()
+        out = p.to(torch.bfloat16).float()
+        if which == 1:
+            n0 = int(self.info.n_encoded_padded) * int(self.cfg.width)
+            hi = p[:n0].to(torch.bfloat16).float()
+            out[:n0] = hi + (p[:n0] - hi).to(torch.bfloat16).float()
+            out[n0:n_mlp] = p[n0:n_mlp].to(torch.float16).float()
+        return out
+
     def get_gradients(self):
         import torch
         out = torch.empty(self.n_params, device="cuda", dtype=torch.float32)

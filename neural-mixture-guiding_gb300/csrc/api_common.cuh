@@ -35,8 +35,15 @@ inline nmg_status ensure_smem(const void* kern, size_t bytes) {
   std::lock_guard<std::mutex> lock(mu);
   size_t& have = done[{kern, dev}];
   if (have >= bytes) return NMG_OK;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (optin > 0 && bytes > size_t(optin))
+    return set_error(NMG_ERR_UNSUPPORTED, "kernel needs %zu B of shared memory, the device allows %d B", bytes, optin);
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
-  if (e != cudaSuccess) return set_error(NMG_ERR_CUDA, "shared memory %zu B: %s", bytes, cudaGetErrorString(e));
+  if (e != cudaSuccess) {
+    cudaGetLastError();  // not sticky: keep it from being reported by a later launch check
+    return set_error(NMG_ERR_CUDA, "shared memory %zu B: %s", bytes, cudaGetErrorString(e));
+  }
   have = bytes;
   return NMG_OK;
 }

@@ -16,7 +16,10 @@ struct FusedArgs {
   uint32_t w_bytes;                  // image bytes (multiple of 16)
   uint32_t layer_off[kMaxLayers];    // byte offset of each layer in the image
   int n_layers;
-  int fp16;                          // operands FP16 instead of BF16
+  int fp16;                          // grid table and encoded features FP16 instead of BF16
+  uint32_t fp16_layers;              // bit l: layer l's operands (its weights and input tile) are FP16
+  uint32_t w0_lo_off;                // non-zero: byte offset of a second layer-0 image (the BF16 low
+                                     // parts w - bf16(w)) whose products the first layer adds
   const uint16_t* table;             // 16-bit grid table [entries][F]
   uint32_t lvl_T[kMaxLevels];        // entries per level
   uint32_t lvl_hash;                 // bit l: level l is hashed (res^3 > T, T a power of two)
@@ -40,6 +43,28 @@ struct FusedArgs {
   float* sel;
   int* err;
 };
+
+NMG_D bool layer_fp16(const FusedArgs& a, int l) { return ((a.fp16_layers >> l) & 1u) != 0; }
+
+// Issues the MMAs of layer l (one thread): D[tmem] = A[a_addr] * W_l^T over
+// the kin input columns, both operands K-major core-matrix tiles in shared
+// memory (w_addr: the weight image). With a low-part image for layer 0 the
+// same A also multiplies W0's low parts into the accumulator, which carries
+// W0 = hi + lo to ~16 significant bits on BF16 operands.
+NMG_D void issue_layer(const FusedArgs& a, int l, uint32_t tmem, uint32_t a_addr, uint32_t w_addr, int kin, int nout) {
+  const uint32_t sbo = uint32_t(kin / 8) * 128u;
+  const uint32_t idesc = tc::idesc_f16(kRows, nout, layer_fp16(a, l));
+  const uint32_t b_addr = w_addr + a.layer_off[l];
+  for (int kk = 0; kk < kin / 16; ++kk)
+    tc::mma_f16(tmem, tc::smem_desc(a_addr + kk * 256u, 128u, sbo), tc::smem_desc(b_addr + kk * 256u, 128u, sbo),
+                idesc, kk > 0 ? 1u : 0u);
+  if (l == 0 && a.w0_lo_off) {
+    const uint32_t lo_addr = w_addr + a.w0_lo_off;
+    for (int kk = 0; kk < kin / 16; ++kk)
+      tc::mma_f16(tmem, tc::smem_desc(a_addr + kk * 256u, 128u, sbo), tc::smem_desc(lo_addr + kk * 256u, 128u, sbo),
+                  idesc, 1u);
+  }
+}
 
 NMG_D int fused_count(const int* d_count, int n_max) {
   if (!d_count) return n_max;
@@ -400,18 +425,25 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
 }
 
 // ------------------------------------------------------------ weight image
+// Image 0 holds the training weights, image 1 the inference weights; each
+// layer l of image i is converted to FP16 when bit l of fp16_layers[i] is
+// set, else to BF16, and image i carries W0's BF16 low parts at w0_lo_off[i]
+// when that is non-zero.
 struct PackArgs {
   long off[kMaxLayers + 1];
   int in[kMaxLayers];
   uint32_t layer_off[kMaxLayers];
   int n_layers;
+  uint32_t fp16_layers[2];
+  uint32_t w0_lo_off[2];
 };
 
 struct FusedState {
   uint8_t* img_train;
   uint8_t* img_infer;
   int* err;
-  uint32_t w_bytes;
+  uint32_t w_bytes;      // training image
+  uint32_t w_bytes_inf;  // inference image
   PackArgs pack;
   int preset;  // 0 none, 1 hash-grid K8, 2 hash-grid K16, 3 reference K8
 };

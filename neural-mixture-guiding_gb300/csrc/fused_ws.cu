@@ -127,7 +127,6 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
   }
   const int n = fused_count(a.d_count, a.n_max);
   const long ntiles = (long(n) + kRows - 1) / kRows;
-  const bool fp16 = a.fp16 != 0;
   bool ok = true;
 
   if (wg < kWsEncoders) {
@@ -173,14 +172,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
     uint32_t phase = 0;
     // Issues layer l's MMAs (one elected thread): A = `a_addr` tile of kin columns.
     auto issue = [&](int l, uint32_t a_addr) {
-      const int kin = l == 0 ? NENC : kWidth;
-      const int nout = l == nl - 1 ? a.n_out_pad : kWidth;
-      const uint32_t sbo = uint32_t(kin / 8) * 128u;
-      const uint32_t idesc = tc::idesc_f16(kRows, nout, fp16);
-      const uint32_t b_addr = w_addr + a.layer_off[l];
-      for (int kk = 0; kk < kin / 16; ++kk)
-        tc::mma_f16(tmem, tc::smem_desc(a_addr + kk * 256u, 128u, sbo), tc::smem_desc(b_addr + kk * 256u, 128u, sbo),
-                    idesc, kk > 0 ? 1u : 0u);
+      issue_layer(a, l, tmem, a_addr, w_addr, l == 0 ? NENC : kWidth, l == nl - 1 ? a.n_out_pad : kWidth);
     };
     // Every exit below follows a bar.red over the group (or depends only on
     // j), so the 128 threads always leave together. (Issuing the next tile's
@@ -219,7 +211,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
           for (int cc = 0; cc < kWidth / 16; ++cc) tc::tmem_ld16(lane_addr + cc * 16, v + 16 * cc);
           tc::tmem_wait_ld();
 #pragma unroll
-          for (int cc = 0; cc < kWidth / 8; ++cc) store_chunk_relu(H, t, cc, kWidth / 8, v + 8 * cc, fp16);
+          for (int cc = 0; cc < kWidth / 8; ++cc) store_chunk_relu(H, t, cc, kWidth / 8, v + 8 * cc, layer_fp16(a, l + 1));
           tc::fence_proxy_async();
           tc::fence_before_sync();
           ok = bar_red_and(bar, kRows, d);

@@ -169,8 +169,8 @@ NMG_D void bar_sync(int id, int count) { asm volatile("bar.sync %0, %1;" ::"r"(i
 // max(a,0), max(b,0) packed into one bf16x2 / f16x2 word in one instruction.
 NMG_D uint32_t pack2_relu(float a, float b, bool fp16) {
   uint32_t r;
-  if (fp16)
-    asm("cvt.rn.relu.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+  if (fp16)  // saturating: a value beyond the FP16 range becomes +-65504, not infinity
+    asm("cvt.rn.satfinite.relu.f16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
   else
     asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
   return r;

@@ -57,6 +57,8 @@ def lib():
         L.nmgo_featurize.argtypes = [C.POINTER(Net), C.c_long, P, P, P, P, P, P]
         L.nmgo_network_forward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P]
         L.nmgo_network_backward.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P, P]
+        L.nmgo_network_forward_f32.argtypes = [C.POINTER(Net), P, C.c_long, P, P]
+        L.nmgo_network_backward_f32.argtypes = [C.POINTER(Net), P, C.c_long, P, P, P]
         L.nmgo_grid_backward.argtypes = [C.POINTER(Net), C.c_long, P, P, P]
         L.nmgo_adam_ema.argtypes = [C.c_long, C.c_long, P, C.c_float, C.c_float, C.c_float, C.c_float,
                                     C.c_float, C.c_float, C.c_float, C.c_uint32, P, P, P, P, P]
@@ -141,6 +143,24 @@ def network_forward(net, params, inputs, want_enc=False):
     enc = np.zeros((n, net.n_enc_padded), np.float64) if want_enc else None
     lib().nmgo_network_forward(C.byref(net), _p(params), n, _p(inputs), _p(raw), _p(enc))
     return (raw, enc) if want_enc else raw
+
+
+def network_forward_f32(net, params, inputs):
+    """The network forward in FP32 arithmetic (the CPU baseline's restatement; FP64 is the oracle)."""
+    params, inputs = _f32(params), _f32(inputs)
+    n = inputs.shape[0]
+    raw = np.zeros((n, net.n_out_padded), np.float32)
+    lib().nmgo_network_forward_f32(C.byref(net), _p(params), n, _p(inputs), _p(raw))
+    return raw
+
+
+def network_backward_f32(net, params, inputs, draw):
+    """dL/dparams of the network in FP32 arithmetic (the CPU baseline's restatement)."""
+    params, inputs, draw = _f32(params), _f32(inputs), _f32(draw)
+    n = inputs.shape[0]
+    dparams = np.zeros(net.n_params, np.float32)
+    lib().nmgo_network_backward_f32(C.byref(net), _p(params), n, _p(inputs), _p(draw), _p(dparams))
+    return dparams
 
 
 def network_backward(net, params, inputs, draw, want_denc=False):

@@ -272,102 +272,116 @@ extern "C" void nmgo_featurize(const nmgo_net* net, long n, const float* pos, co
   }
 }
 
-// Composite encoding of one input row into enc[n_enc_padded] (FP64).
-static void encode_row(const nmgo_net* net, const GridSpec& g, const float* table, const float* x,
-                       double* enc) {
-  grid_encode<double>(g, table, x, enc);
+// The network forward and backward are templated on the arithmetic type S:
+// double is the FP64 parity oracle, float the FP32 restatement that the CPU
+// baseline times (the reference has no CPU implementation of the network).
+
+// Composite encoding of one input row into enc[n_enc_padded].
+template <class S>
+static void encode_row(const nmgo_net* net, const GridSpec& g, const float* table, const float* x, S* enc) {
+  grid_encode<S>(g, table, x, enc);
   int o = net->grid_levels * net->grid_feats;
   int d2 = net->sh_degree * net->sh_degree;
-  double sh[16];
-  sh_encode<double>(net->sh_degree, double(x[3] * 2.0f - 1.0f), double(x[4] * 2.0f - 1.0f),
-                    double(x[5] * 2.0f - 1.0f), sh);
+  S sh[16];
+  sh_encode<S>(net->sh_degree, S(x[3] * 2.0f - 1.0f), S(x[4] * 2.0f - 1.0f), S(x[5] * 2.0f - 1.0f), sh);
   for (int k = 0; k < d2; ++k) enc[o + k] = sh[k];
   o += d2;
   if (net->input_mode == 0) {
     for (int d = 6; d < 9; ++d) {
-      oneblob_encode<double>(net->oneblob_bins, double(x[d]), enc + o);
+      oneblob_encode<S>(net->oneblob_bins, S(x[d]), enc + o);
       o += net->oneblob_bins;
     }
   } else {
-    sh_encode<double>(net->sh_degree, double(x[6] * 2.0f - 1.0f), double(x[7] * 2.0f - 1.0f),
-                      double(x[8] * 2.0f - 1.0f), sh);
+    sh_encode<S>(net->sh_degree, S(x[6] * 2.0f - 1.0f), S(x[7] * 2.0f - 1.0f), S(x[8] * 2.0f - 1.0f), sh);
     for (int k = 0; k < d2; ++k) enc[o + k] = sh[k];
     o += d2;
-    oneblob_encode<double>(net->oneblob_bins, double(x[9]), enc + o);
+    oneblob_encode<S>(net->oneblob_bins, S(x[9]), enc + o);
     o += net->oneblob_bins;
   }
-  for (; o < net->n_enc_padded; ++o) enc[o] = 1.0;
+  for (; o < net->n_enc_padded; ++o) enc[o] = S(1);
 }
 
 // y[rows] = W[rows x cols] * x[cols]
-static void matvec(const float* W, int rows, int cols, const double* x, double* y) {
+template <class S>
+static void matvec(const float* W, int rows, int cols, const S* x, S* y) {
   for (int r = 0; r < rows; ++r) {
-    double acc = 0;
-    for (int c = 0; c < cols; ++c) acc += double(W[(long)r * cols + c]) * x[c];
+    S acc = 0;
+    for (int c = 0; c < cols; ++c) acc += S(W[(long)r * cols + c]) * x[c];
     y[r] = acc;
   }
 }
 
+template <class S>
 struct Fwd {
-  double enc[256];
-  double h[8][128];  // hidden activations after ReLU
-  double y[256];
+  S enc[256];
+  S h[8][128];  // hidden activations after ReLU
+  S y[256];
 };
 
-static void forward_row(const nmgo_net* net, const GridSpec& g, const float* params, const float* x,
-                        Fwd& f) {
+template <class S>
+static void forward_row(const nmgo_net* net, const GridSpec& g, const float* params, const float* x, Fwd<S>& f) {
   const float* W = params;
   const float* table = params + net->n_mlp_params;
-  encode_row(net, g, table, x, f.enc);
-  const double* in = f.enc;
+  encode_row<S>(net, g, table, x, f.enc);
+  const S* in = f.enc;
   int in_w = net->n_enc_padded;
   for (int l = 0; l < net->n_hidden; ++l) {
-    matvec(W, net->width, in_w, in, f.h[l]);
-    for (int k = 0; k < net->width; ++k) f.h[l][k] = std::max(0.0, f.h[l][k]);
+    matvec<S>(W, net->width, in_w, in, f.h[l]);
+    for (int k = 0; k < net->width; ++k) f.h[l][k] = std::max(S(0), f.h[l][k]);
     W += (long)net->width * in_w;
     in = f.h[l];
     in_w = net->width;
   }
-  matvec(W, net->n_out_padded, net->width, in, f.y);
+  matvec<S>(W, net->n_out_padded, net->width, in, f.y);
 }
 
 // Network forward: inputs [n x n_input] -> raw outputs [n x n_out_padded]
 // (optionally also the encoded inputs [n x n_enc_padded]).
-extern "C" void nmgo_network_forward(const nmgo_net* net, const float* params, long n, const float* inputs,
-                          double* raw, double* enc_out) {
+template <class S>
+static void network_forward(const nmgo_net* net, const float* params, long n, const float* inputs, S* raw,
+                            S* enc_out) {
   GridSpec g = grid_of(net);
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < n; ++i) {
-    Fwd f;
-    forward_row(net, g, params, inputs + i * net->n_input, f);
+    Fwd<S> f;
+    forward_row<S>(net, g, params, inputs + i * net->n_input, f);
     for (int k = 0; k < net->n_out_padded; ++k) raw[i * net->n_out_padded + k] = f.y[k];
     if (enc_out)
       for (int k = 0; k < net->n_enc_padded; ++k) enc_out[i * net->n_enc_padded + k] = f.enc[k];
   }
 }
+extern "C" void nmgo_network_forward(const nmgo_net* net, const float* params, long n, const float* inputs,
+                                     double* raw, double* enc_out) {
+  network_forward<double>(net, params, n, inputs, raw, enc_out);
+}
+extern "C" void nmgo_network_forward_f32(const nmgo_net* net, const float* params, long n, const float* inputs,
+                                         float* raw) {
+  network_forward<float>(net, params, n, inputs, raw, nullptr);
+}
 
 // grid_backward with OpenMP atomic accumulation (same weights as the forward).
-static void grid_backward_atomic(const GridSpec& g, const float pos[3], const double* dfeat, double* grad) {
+template <class S>
+static void grid_backward_atomic(const GridSpec& g, const float pos[3], const S* dfeat, S* grad) {
   float l2s = std::log2(g.per_level_scale);
   for (int l = 0; l < g.levels; ++l) {
     float scale = grid_scale(uint32_t(l), l2s, uint32_t(g.base_res));
     uint32_t res = grid_resolution(scale);
     uint32_t T = g.offset[l + 1] - g.offset[l];
-    double w[3];
+    S w[3];
     uint32_t pg[3];
     for (int d = 0; d < 3; ++d) {
       float p = pos[d] * scale + 0.5f;
       float fl = floorf(p);
       pg[d] = uint32_t(int(fl));
-      double f = double(p - fl);
-      w[d] = g.smoothstep ? f * f * (3.0 - 2.0 * f) : f;
+      S f = S(p - fl);
+      w[d] = g.smoothstep ? f * f * (S(3) - S(2) * f) : f;
     }
     for (int c = 0; c < 8; ++c) {
-      double wt = 1;
+      S wt = 1;
       uint32_t lp[3];
       for (int d = 0; d < 3; ++d) {
         if ((c & (1 << d)) == 0) {
-          wt *= 1.0 - w[d];
+          wt *= S(1) - w[d];
           lp[d] = pg[d];
         } else {
           wt *= w[d];
@@ -384,25 +398,26 @@ static void grid_backward_atomic(const GridSpec& g, const float pos[3], const do
 }
 
 // Network backward: dL/draw [n x n_out_padded] -> dL/dparams (accumulated,
-// FP64, same layout as params) and optionally dL/dencoded [n x n_enc_padded].
-extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, long n, const float* inputs,
-                           const double* draw, double* dparams, double* denc_out) {
+// same layout as params) and optionally dL/dencoded [n x n_enc_padded].
+template <class S>
+static void network_backward(const nmgo_net* net, const float* params, long n, const float* inputs, const S* draw,
+                             S* dparams, S* denc_out) {
   GridSpec g = grid_of(net);
   int nt = nmgo_num_threads();
   // MLP gradient: per-thread partials (small); grid gradient: atomic adds
   // straight into dparams (the table is large and sparsely touched).
-  std::vector<std::vector<double>> part(nt, std::vector<double>(net->n_mlp_params, 0.0));
-  double* dgrid = dparams + net->n_mlp_params;
+  std::vector<std::vector<S>> part(nt, std::vector<S>(net->n_mlp_params, S(0)));
+  S* dgrid = dparams + net->n_mlp_params;
 #pragma omp parallel for schedule(static)
   for (long i = 0; i < n; ++i) {
 #ifdef _OPENMP
-    std::vector<double>& acc = part[omp_get_thread_num()];
+    std::vector<S>& acc = part[omp_get_thread_num()];
 #else
-    std::vector<double>& acc = part[0];
+    std::vector<S>& acc = part[0];
 #endif
-    Fwd f;
+    Fwd<S> f;
     const float* x = inputs + i * net->n_input;
-    forward_row(net, g, params, x, f);
+    forward_row<S>(net, g, params, x, f);
     // weight offsets
     long off[10];
     off[0] = 0;
@@ -411,7 +426,7 @@ extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, 
       off[l + 1] = off[l] + (long)net->width * in_w;
       in_w = net->width;
     }
-    double d[256], dn[256];
+    S d[256], dn[256];
     for (int k = 0; k < net->n_out_padded; ++k) d[k] = draw[i * net->n_out_padded + k];
     // output layer
     int L = net->n_hidden;
@@ -420,30 +435,38 @@ extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, 
       for (int r = 0; r < net->n_out_padded; ++r)
         for (int c = 0; c < net->width; ++c) acc[off[L] + (long)r * net->width + c] += d[r] * f.h[L - 1][c];
       for (int c = 0; c < net->width; ++c) {
-        double s = 0;
-        for (int r = 0; r < net->n_out_padded; ++r) s += double(W[(long)r * net->width + c]) * d[r];
-        dn[c] = f.h[L - 1][c] > 0 ? s : 0.0;
+        S s = 0;
+        for (int r = 0; r < net->n_out_padded; ++r) s += S(W[(long)r * net->width + c]) * d[r];
+        dn[c] = f.h[L - 1][c] > 0 ? s : S(0);
       }
     }
     for (int l = L - 1; l >= 0; --l) {
       for (int c = 0; c < net->width; ++c) d[c] = dn[c];
-      const double* in = l == 0 ? f.enc : f.h[l - 1];
+      const S* in = l == 0 ? f.enc : f.h[l - 1];
       int iw = l == 0 ? net->n_enc_padded : net->width;
       const float* W = params + off[l];
       for (int r = 0; r < net->width; ++r)
         for (int c = 0; c < iw; ++c) acc[off[l] + (long)r * iw + c] += d[r] * in[c];
       for (int c = 0; c < iw; ++c) {
-        double s = 0;
-        for (int r = 0; r < net->width; ++r) s += double(W[(long)r * iw + c]) * d[r];
-        dn[c] = (l == 0) ? s : (f.h[l - 1][c] > 0 ? s : 0.0);
+        S s = 0;
+        for (int r = 0; r < net->width; ++r) s += S(W[(long)r * iw + c]) * d[r];
+        dn[c] = (l == 0) ? s : (f.h[l - 1][c] > 0 ? s : S(0));
       }
     }
     if (denc_out)
       for (int k = 0; k < net->n_enc_padded; ++k) denc_out[i * net->n_enc_padded + k] = dn[k];
-    grid_backward_atomic(g, x, dn, dgrid);
+    grid_backward_atomic<S>(g, x, dn, dgrid);
   }
   for (int t = 0; t < nt; ++t)
     for (long k = 0; k < net->n_mlp_params; ++k) dparams[k] += part[t][k];
+}
+extern "C" void nmgo_network_backward(const nmgo_net* net, const float* params, long n, const float* inputs,
+                                      const double* draw, double* dparams, double* denc_out) {
+  network_backward<double>(net, params, n, inputs, draw, dparams, denc_out);
+}
+extern "C" void nmgo_network_backward_f32(const nmgo_net* net, const float* params, long n, const float* inputs,
+                                          const float* draw, float* dparams) {
+  network_backward<float>(net, params, n, inputs, draw, dparams, nullptr);
 }
 
 // Adam (adam.h:47-119) followed by EMA (ema.h:62-75,102-145) over all params.
@@ -477,5 +500,6 @@ extern "C" void nmgo_adam_ema(long n_params, long n_matrix, const float* grad, f
 extern "C" void nmgo_grid_backward(const nmgo_net* net, long n, const float* inputs, const double* denc, double* dgrid) {
   GridSpec g = grid_of(net);
 #pragma omp parallel for schedule(static)
-  for (long i = 0; i < n; ++i) grid_backward_atomic(g, inputs + i * net->n_input, denc + i * net->n_enc_padded, dgrid);
+  for (long i = 0; i < n; ++i)
+    grid_backward_atomic<double>(g, inputs + i * net->n_input, denc + i * net->n_enc_padded, dgrid);
 }

@@ -2,9 +2,11 @@
 accumulate) against the FP64 oracle.
 
   * raw network outputs: compared with the FP64 oracle evaluated on the
-    same 16-bit-rounded weights and grid table, so the remaining difference
-    is the rounding of encoded features and hidden activations to 16 bits
-    (2^-9 relative for BF16, 2^-11 for FP16) accumulated over the layers:
+    parameter values the kernels multiply (GuidingField.operand_params: the
+    16-bit grid table; for the BF16 path's query image W0 as a BF16 hi + lo
+    pair and FP16 later layers), so the remaining difference is the rounding
+    of encoded features and hidden activations to 16 bits (2^-9 relative for
+    BF16, 2^-11 for FP16) accumulated over the layers:
     max |err| <= 4e-2 (BF16) / 1e-2 (FP16) of max |y|, RMS <= 6e-3 / 2e-3 of RMS y.
     A wrong operand layout or descriptor gives O(1) errors.
   * mixture stage (fast-math FP32 on the fused kernel's own raw outputs):
@@ -59,7 +61,7 @@ def test_fused_raw_outputs(field, oracle, synth):
     q = synth.wavefront(16384, seed=11)
     x = synth.featurize(q, f.cfg.input_mode)
     raw = f.infer_raw(dev(x)[0], which=1).cpu().numpy()
-    w16 = round16(f.get_params(1).cpu().numpy(), fp16)
+    w16 = f.operand_params(1).cpu().numpy()
     raw64 = oracle.network_forward(net, w16, x)
     nu = net.n_out_padded
     err = np.abs(raw[:, :nu] - raw64[:, :nu])
@@ -321,9 +323,17 @@ def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
     q = synth.wavefront(50000, seed=21)
     pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
     ref = None
+    ran = []
     for wg in (4, 5, 6, 8, 9, 10, 11, 12):
         f.set_query_tiling(wg)
-        out = f.query(pos, wo, n, r, u4, want_raw=True)
+        try:
+            out = f.query(pos, wo, n, r, u4, want_raw=True)
+        except nmg.NMGError as e:
+            # a tiling whose shared memory does not fit this network's weight image (the 8-slot ring
+            # with the BF16 path's extra layer-0 image) reports UNSUPPORTED and is skipped
+            assert e.status == 6, e
+            continue
+        ran.append(wg)
         if ref is None:
             ref = out
         else:
@@ -336,8 +346,9 @@ def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
             assert float(((out["dir"] - ref["dir"])[same]).pow(2).mean().sqrt()) <= 1e-3, wg
             rel = (out["pdf"] - ref["pdf"])[same].abs() / ref["pdf"][same]
             assert float(rel.pow(2).mean().sqrt()) <= 1e-3, wg
+    assert len(ran) >= 6 and 12 in ran and 4 in ran
     chosen = f.autotune(pos, wo, n, r, u4, use_cache=True)
-    assert chosen in (4, 5, 6, 8, 9, 10, 11, 12) and f.query_tiling == chosen
+    assert chosen in ran and f.query_tiling == chosen
     assert (tmp_path / "tune.txt").read_text().strip().endswith(str(chosen))
     f.set_query_tiling(0)
     assert f.autotune(pos, wo, n, r, u4, use_cache=True) == chosen  # served from the cache
