@@ -243,6 +243,17 @@ def config(preset=PRESET_HASHGRID, **overrides):
     return cfg
 
 
+def config_info(cfg):
+    """nmg_config_info: the sizes a configuration implies (no device needed)."""
+    L = lib()
+    if not hasattr(L, "_field_bound"):
+        _bind_field(L)
+        L._field_bound = True
+    info = Info()
+    check(L.nmg_config_info(C.byref(cfg), C.byref(info)))
+    return info
+
+
 class GuidingField:
     """The network-backed guiding distribution (encoding -> MLP -> vMF mixture).
 

@@ -344,7 +344,8 @@ __global__ void __launch_bounds__(256) k_adam_ema(AdamArgs a, const float4* __re
         mm[k] = a.beta1 * mm[k] + (1.f - a.beta1) * g;
         vv[k] = a.beta2 * vv[k] + (1.f - a.beta2) * (g * g);
         const uint32_t t = ++tt[k];
-        const float lr_t = a.lr * sqrtf(1.f - exp2f(float(t) * a.log2_beta2)) / (1.f - exp2f(float(t) * a.log2_beta1));
+        // adam.h:102: the bias-correction quotient first, then the learning rate
+        const float lr_t = a.lr * (sqrtf(1.f - exp2f(float(t) * a.log2_beta2)) / (1.f - exp2f(float(t) * a.log2_beta1)));
         ww[k] = ww[k] - lr_t / (sqrtf(vv[k]) + a.eps) * mm[k];
       }
       m[j] = make_float4(mm[0], mm[1], mm[2], mm[3]);

@@ -206,6 +206,16 @@ def ref_lib():
         L.ref_generate_training_data.restype = C.c_int
         L.ref_generate_inference_data.argtypes = [P, P, P, P, C.c_int, P, P, P, P, P, P]
         L.ref_generate_inference_data.restype = C.c_int
+        U = C.c_uint32
+        L.ref_tcnn_grid_forward.argtypes = [C.c_int, C.c_int, P, U, C.c_float, C.c_int, C.c_int, P, P, U, P]
+        L.ref_tcnn_grid_backward.argtypes = [C.c_int, C.c_int, P, U, C.c_float, C.c_int, C.c_int, P, U, P, P]
+        L.ref_tcnn_grid_layout.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, P, P]
+        L.ref_tcnn_snapshot_msgpack.argtypes = [P, C.c_uint64, C.c_int, P, C.c_long]
+        L.ref_tcnn_snapshot_msgpack.restype = C.c_long
+        L.ref_tcnn_sh.argtypes = [U, P, U, P]
+        L.ref_tcnn_oneblob.argtypes = [U, P, U, U, P]
+        L.ref_tcnn_adam_ema.argtypes = [U, U, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                        C.c_float, U, C.c_int, P, P, P, P, P, P, P, P]
         _ref = L
     return _ref
 
@@ -353,3 +363,89 @@ def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_
                     outs.append(o)
     ni = 9 if input_mode == 0 else 10
     return (np.array(xs, np.float32).reshape(-1, ni), np.array(outs, np.float32).reshape(-1, 7 if selection else 6))
+
+
+# ---------------------------------------------------------------------------
+# tiny-cuda-nn 1.7's own kernels run on the host (oracle/ref_tcnn_kernels.cu):
+# golden vectors for the encodings and the optimiser.
+# ---------------------------------------------------------------------------
+def ref_tcnn_grid_forward(feats, offsets, base_res, per_level_scale, hash_, smoothstep, table, pos):
+    """kernel_grid (grid.h:220-384): features [n, levels * feats] of positions [n, 3] for a float table
+    [offsets[-1] * feats]."""
+    offsets = np.ascontiguousarray(offsets, np.uint32)
+    levels = len(offsets) - 1
+    pos, table = _f32(pos), _f32(table)
+    n = pos.shape[0]
+    enc = np.zeros((levels * feats, n), np.float32)
+    r = ref_lib().ref_tcnn_grid_forward(feats, levels, _p(offsets), base_res, per_level_scale, int(hash_),
+                                        int(smoothstep), _p(table), _p(pos), n, _p(enc))
+    assert r == 0
+    return np.ascontiguousarray(enc.T)
+
+
+def ref_tcnn_grid_backward(feats, offsets, base_res, per_level_scale, hash_, smoothstep, pos, dl_dy):
+    """kernel_grid_backward (grid.h:386-510): table gradient [offsets[-1] * feats] of dL/dfeatures
+    dl_dy [n, levels * feats] at positions [n, 3] (FP32 accumulation, as tcnn's float gradient path)."""
+    offsets = np.ascontiguousarray(offsets, np.uint32)
+    levels = len(offsets) - 1
+    pos = _f32(pos)
+    n = pos.shape[0]
+    dl = np.ascontiguousarray(np.asarray(dl_dy, np.float32).T)
+    grad = np.zeros(int(offsets[-1]) * feats, np.float32)
+    r = ref_lib().ref_tcnn_grid_backward(feats, levels, _p(offsets), base_res, per_level_scale, int(hash_),
+                                         int(smoothstep), _p(pos), n, _p(dl), _p(grad))
+    assert r == 0
+    return grad
+
+
+def ref_tcnn_sh(degree, x01):
+    """kernel_sh (spherical_harmonics.h:126-153) of rows (d + 1) / 2: [n, degree^2]."""
+    x01 = _f32(x01)
+    n = x01.shape[0]
+    out = np.zeros((n, degree * degree), np.float32)
+    ref_lib().ref_tcnn_sh(degree, _p(x01), n, _p(out))
+    return out
+
+
+def ref_tcnn_oneblob(bins, vals):
+    """kernel_one_blob_soa (oneblob.h:98-127): vals [n, dims] -> [n, dims * bins] (dimension-major)."""
+    vals = _f32(vals)
+    n, dims = vals.shape
+    out = np.zeros((dims * bins, n), np.float32)
+    ref_lib().ref_tcnn_oneblob(int(bins).bit_length() - 1, _p(vals), n, dims, _p(out))
+    return np.ascontiguousarray(out.T)
+
+
+def ref_tcnn_adam_ema(state, grad16, n_matrix, step, loss_scale=128.0, lr=1e-2, beta1=0.9, beta2=0.99, eps=1e-15,
+                      l2_reg=1e-6, ema_decay=0.95, full_precision=True):
+    """One EMA(Adam) step of tcnn (adam.h:47-119, ema.h:44-76) on `state` (dict of float32 arrays w_full, w16,
+    m, v, ema16, ema_tmp and uint32 psteps, updated in place); grad16 holds the __half gradients as float."""
+    n = state["w_full"].size
+    grad16 = _f32(grad16)
+    ref_lib().ref_tcnn_adam_ema(n, n_matrix, loss_scale, lr, beta1, beta2, eps, l2_reg, ema_decay, step,
+                                int(full_precision), _p(state["w_full"]), _p(state["w16"]), _p(grad16),
+                                _p(state["m"]), _p(state["v"]), _p(state["psteps"]), _p(state["ema16"]),
+                                _p(state["ema_tmp"]))
+    return state
+
+
+def ref_tcnn_grid_layout(feats, levels, log2_hashmap, base_res, per_level_scale, hash_, smoothstep):
+    """tcnn's GridEncodingTemplated constructor (grid.h:939-1000): the entry offset of every level
+    [levels + 1] and the parameter count."""
+    offsets = np.zeros(levels + 1, np.uint32)
+    n_params = np.zeros(1, np.uint64)
+    r = ref_lib().ref_tcnn_grid_layout(feats, levels, log2_hashmap, base_res, per_level_scale, int(hash_),
+                                       int(smoothstep), _p(offsets), _p(n_params))
+    assert r == 0
+    return offsets, int(n_params[0])
+
+
+def ref_tcnn_snapshot(params, params_type="__half"):
+    """The bytes of a tcnn Trainer snapshot (Trainer::serialize, trainer.h:267-278, encoded by the reference's
+    nlohmann::json::to_msgpack) holding `params` as __half or float."""
+    p = np.ascontiguousarray(params, np.float16 if params_type == "__half" else np.float32)
+    cap = p.nbytes + 256
+    out = np.zeros(cap, np.uint8)
+    n = ref_lib().ref_tcnn_snapshot_msgpack(_p(p), p.size, 0 if params_type == "__half" else 1, _p(out), cap)
+    assert n > 0
+    return out[:n].tobytes()

@@ -43,7 +43,8 @@ def build_reference():
     if not os.path.isdir(os.path.join(ref, "src", "render", "guided")):
         return None
     out = os.path.join(HERE, "_ref", "libnmgref.so")
-    srcs = [os.path.join(HERE, "ref_shim.cu"), script]
+    srcs = [os.path.join(HERE, f) for f in ("ref_shim.cu", "ref_tcnn_kernels.cu", "ref_tcnn_layout.cu",
+                                            "tcnn_host_headers.py")] + [script]
     if os.path.exists(out) and all(os.path.getmtime(p) <= os.path.getmtime(out) for p in srcs):
         return out
     subprocess.run(["bash", script], check=True, stdout=subprocess.DEVNULL)

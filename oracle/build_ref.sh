@@ -15,6 +15,8 @@
 #   core/mesh.h, core/scenegraph.h  Eigen Affine3f copy-init rejected by g++ 13
 #                                   (default-initialised instead; unused here)
 # plus soac-generated SOA headers and a config.h written from config.in.h.
+# tiny-cuda-nn's kernel headers get host-callable copies of their own
+# (tcnn_host_headers.py) for oracle/ref_tcnn_kernels.cu.
 # krr::Primes (a device table of util/tables.cpp that the host pass cannot
 # define) gets a host stub; the Halton sampler that reads it is not used.
 set -euo pipefail
@@ -68,5 +70,21 @@ printf 'namespace krr { extern const int Primes[1000]; const int Primes[1000] = 
 nvcc -std=c++17 -arch=sm_90 -DTCNN_MIN_GPU_ARCH=90 --extended-lambda --expt-relaxed-constexpr \
   -Xcompiler -fPIC,-ffp-contract=off -D'__assume(x)=' $INC -c "$HERE/ref_shim.cu" -o "$B/ref_shim.o"
 g++ -fPIC -c "$B/primes_stub.cpp" -o "$B/primes_stub.o"
-nvcc -shared -arch=sm_90 "$B/ref_shim.o" "$B/primes_stub.o" -o "$OUT/libnmgref.so"
+
+# 5. tcnn's encoding and optimiser kernels as host functions: host-callable
+#    copies of their headers (cut before the classes, qualifiers widened; see
+#    tcnn_host_headers.py) ahead of the originals on the include path
+rm -rf "$B/tcnn_host"
+python3 "$HERE/tcnn_host_headers.py" "$T/include" "$B/tcnn_host"
+TINC="-I$B/tcnn_host -I$T/include -I$T/dependencies -I$T/dependencies/fmt/include"
+nvcc -std=c++17 -arch=sm_90 -DTCNN_MIN_GPU_ARCH=90 --extended-lambda --expt-relaxed-constexpr \
+  -Xcompiler -fPIC,-ffp-contract=off $TINC -c "$HERE/ref_tcnn_kernels.cu" -o "$B/ref_tcnn_kernels.o"
+# 6. tcnn's own grid-encoding constructor (level offsets, parameter count) from
+#    the unmodified headers, with the vendored fmt's format.cc
+TCI="-I$T/include -I$T/dependencies -I$T/dependencies/fmt/include"
+nvcc -std=c++17 -arch=sm_90 -DTCNN_MIN_GPU_ARCH=90 --extended-lambda --expt-relaxed-constexpr \
+  -Xcompiler -fPIC $TCI -c "$HERE/ref_tcnn_layout.cu" -o "$B/ref_tcnn_layout.o"
+g++ -std=c++17 -O1 -fPIC -I"$T/dependencies/fmt/include" -c "$T/dependencies/fmt/src/format.cc" -o "$B/fmt_format.o"
+nvcc -shared -arch=sm_90 "$B/ref_shim.o" "$B/primes_stub.o" "$B/ref_tcnn_kernels.o" "$B/ref_tcnn_layout.o" \
+  "$B/fmt_format.o" -o "$OUT/libnmgref.so"
 echo "built $OUT/libnmgref.so"

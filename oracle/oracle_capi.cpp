@@ -487,7 +487,8 @@ extern "C" void nmgo_adam_ema(long n_params, long n_matrix, const float* grad, f
       float mm = m[i] = beta1 * m[i] + (1.0f - beta1) * g;
       float vv = v[i] = beta2 * v[i] + (1.0f - beta2) * (g * g);
       uint32_t t = ++psteps[i];
-      float lr_t = lr * sqrtf(1.0f - powf(beta2, (float)t)) / (1.0f - powf(beta1, (float)t));
+      // adam.h:102: learning_rate *= sqrtf(1 - beta2^t) / (1 - beta1^t), the quotient first
+      float lr_t = lr * (sqrtf(1.0f - powf(beta2, (float)t)) / (1.0f - powf(beta1, (float)t)));
       float eff = lr_t / (sqrtf(vv) + eps);
       w[i] = wf - eff * mm;
     }

@@ -212,6 +212,100 @@ def train_cu():
     print("wrote", path, "records", len(x), "queries", len(fx), "bytes", os.path.getsize(path))
 
 
+# ---------------------------------------------------------------------------
+# tcnn_golden.npz: tiny-cuda-nn 1.7's own code (oracle/ref_tcnn_kernels.cu,
+# oracle/ref_tcnn_layout.cu) on seeded inputs, for both network presets:
+#   layout    -- GridEncodingTemplated's level offsets and parameter count
+#   grid      -- kernel_grid features and kernel_grid_backward table gradients
+#                for a table given by a fixed integer formula (table_values)
+#   sh, oneblob -- kernel_sh (degrees 2 and 4) and kernel_one_blob_soa (4 bins)
+#   adam      -- three EMA(Adam) steps (adam_step + full- and half-precision EMA)
+#                with the reference's optimiser settings (base.json)
+#   snapshot  -- Trainer::serialize + nlohmann to_msgpack of a small network's
+#                parameters, as __half and as float
+# ---------------------------------------------------------------------------
+def table_values(n):
+    """The grid table both the fixture and its tests use: ((i * 2654435761) mod 2^32) / 2^32 - 0.5."""
+    i = np.arange(n, dtype=np.uint64)
+    return (((i * np.uint64(2654435761)) % np.uint64(1 << 32)).astype(np.float64) / 2.0 ** 32 - 0.5).astype(np.float32)
+
+
+SNAPSHOT_CONFIG = dict(grid_levels=2, grid_base_resolution=4)  # on NMG_PRESET_REFERENCE: 13,408 parameters
+
+
+def grid_positions(rng, res0, n=256):
+    pos = rng.random((n, 3)).astype(np.float32)
+    pos[:8] = np.array([[x, y, z] for x in (0, 1) for y in (0, 1) for z in (0, 1)], np.float32)
+    pos[8] = 0.5
+    pos[9:12] = np.float32(1.0 / res0) * np.arange(1, 4, dtype=np.float32)[:, None]  # on level-0 vertices
+    pos[12] = np.float32(np.nextafter(np.float32(1), np.float32(0)))
+    return pos
+
+
+def tcnn():
+    nmg = importlib.import_module("neural-mixture-guiding_gb300")
+    rng = np.random.default_rng(SEED + 21)
+    out = {}
+    for preset in (nmg.PRESET_HASHGRID, nmg.PRESET_REFERENCE):
+        cfg = nmg.config(preset)
+        tag = "hash" if preset == nmg.PRESET_HASHGRID else "dense"
+        F, Lv = int(cfg.grid_features), int(cfg.grid_levels)
+        offs, npar = O.ref_tcnn_grid_layout(F, Lv, cfg.grid_log2_hashmap, cfg.grid_base_resolution,
+                                            cfg.grid_per_level_scale, cfg.grid_hash, cfg.grid_smoothstep)
+        table = table_values(int(offs[-1]) * F)
+        pos = grid_positions(rng, cfg.grid_base_resolution)
+        args = (F, offs, cfg.grid_base_resolution, cfg.grid_per_level_scale, cfg.grid_hash, cfg.grid_smoothstep)
+        feats = O.ref_tcnn_grid_forward(*args, table, pos)
+        bpos = pos[:48]
+        dl = rng.standard_normal((len(bpos), Lv * F)).astype(np.float32)
+        g = O.ref_tcnn_grid_backward(*args, bpos, dl)
+        nz = np.nonzero(g)[0].astype(np.int64)
+        out.update({tag + "_offsets": offs, tag + "_n_params": np.int64(npar), tag + "_pos": pos,
+                    tag + "_features": feats, tag + "_bwd_pos": bpos, tag + "_dl_dy": dl,
+                    tag + "_grad_index": nz, tag + "_grad_value": g[nz]})
+    d = synth.uniform_sphere(rng, (256,)).astype(np.float32)
+    d[:6] = np.array([[0, 0, 1], [0, 0, -1], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0]], np.float32)
+    x01 = ((d + 1) * 0.5).astype(np.float32)
+    out["sh_in"] = x01
+    out["sh2"] = O.ref_tcnn_sh(2, x01)
+    out["sh4"] = O.ref_tcnn_sh(4, x01)
+    ob = rng.random((256, 3)).astype(np.float32)
+    ob[:6, 0] = (0.0, 0.25, 0.5, 0.75, np.nextafter(np.float32(1), np.float32(0)), 1.0)
+    out["oneblob_in"] = ob
+    out["oneblob4"] = O.ref_tcnn_oneblob(4, ob)
+    # three optimiser steps on 4,096 parameters, the first 1,024 matrix weights; some non-matrix
+    # gradients are exactly zero (those parameters keep their state)
+    n, n_mat = 4096, 1024
+    w0 = (rng.standard_normal(n) * 0.1).astype(np.float32)
+    grads = []
+    for _ in range(3):
+        gg = (rng.standard_normal(n) * 4.0).astype(np.float16).astype(np.float32)
+        gg[n_mat:][rng.random(n - n_mat) < 0.3] = 0.0
+        grads.append(gg)
+    for full in (True, False):
+        st = {"w_full": w0.copy(), "w16": w0.astype(np.float16).astype(np.float32), "m": np.zeros(n, np.float32),
+              "v": np.zeros(n, np.float32), "psteps": np.zeros(n, np.uint32),
+              "ema16": np.zeros(n, np.float32), "ema_tmp": np.zeros(n, np.float32)}
+        for k in range(3):
+            O.ref_tcnn_adam_ema(st, grads[k], n_mat, k + 1, full_precision=full)
+        key = "adam_full" if full else "adam_half"
+        for name in ("w_full", "m", "v", "psteps", "ema16", "ema_tmp"):
+            out[key + "_" + name] = st[name]
+    out["adam_w0"] = w0
+    out["adam_grads"] = np.stack(grads)
+    out["adam_n_matrix"] = np.int64(n_mat)
+    scfg = nmg.config(nmg.PRESET_REFERENCE, **SNAPSHOT_CONFIG)
+    sn = int(nmg.config_info(scfg).n_params)
+    sp = (table_values(sn) * np.float32(0.2)).astype(np.float32)
+    out["snapshot_n_params"] = np.int64(sn)
+    out["snapshot_half"] = np.frombuffer(O.ref_tcnn_snapshot(sp, "__half"), np.uint8)
+    out["snapshot_float"] = np.frombuffer(O.ref_tcnn_snapshot(sp, "float"), np.uint8)
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tcnn_golden.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, "bytes", os.path.getsize(path))
+
+
 if __name__ == "__main__":
     main()
     train_cu()
+    tcnn()
