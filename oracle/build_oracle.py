@@ -37,17 +37,19 @@ def build(force=False, verbose=False):
 
 
 def build_reference():
-    """Compile the reference's own mixture code (only where its checkout exists)."""
+    """Compile the reference's own code for the oracle (only where its checkout exists: build_ref.sh
+    looks for it, at $NMG_REFERENCE when that is set)."""
     script = os.path.join(HERE, "build_ref.sh")
-    ref = os.environ.get("NMG_REFERENCE", "/root/reference")
-    if not os.path.isdir(os.path.join(ref, "src", "render", "guided")):
+    if subprocess.run(["bash", script, "--check"], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL).returncode:
         return None
     out = os.path.join(HERE, "_ref", "libnmgref.so")
     srcs = [os.path.join(HERE, f) for f in ("ref_shim.cu", "ref_tcnn_kernels.cu", "ref_tcnn_layout.cu",
                                             "tcnn_host_headers.py")] + [script]
     if os.path.exists(out) and all(os.path.getmtime(p) <= os.path.getmtime(out) for p in srcs):
         return out
-    subprocess.run(["bash", script], check=True, stdout=subprocess.DEVNULL)
+    r = subprocess.run(["bash", script], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("build_ref.sh failed:\n" + r.stderr[-4000:])
     return out
 
 

@@ -26,9 +26,10 @@ OUT=$HERE/_ref
 B=$OUT/build
 SRC=$REF/src
 if [ ! -d "$SRC/render/guided" ]; then
-  echo "reference checkout not found at $REF" >&2
+  echo "reference checkout not found at $REF (set NMG_REFERENCE)" >&2
   exit 3
 fi
+if [ "${1:-}" = "--check" ]; then exit 0; fi
 mkdir -p "$B/gen/render/wavefront" "$B/gen/render/guided"
 
 # 1. soac (SOA code generator) and the two generated headers
