@@ -125,9 +125,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
       tc::fence_after_sync();
       if (!last) {
         float v[kWidth];
-#pragma unroll
-        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(lane_addr + c * 16, v + 16 * c);
-        tc::tmem_wait_ld();
+        tc::tmem_load<kWidth / 16>(lane_addr, v);
 #pragma unroll
         for (int c = 0; c < kWidth / 8; ++c) store_chunk_relu(A, t, c, kWidth / 8, v + 8 * c, layer_fp16(a, l + 1));
         tc::fence_proxy_async();
@@ -136,10 +134,7 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
         if (!ok) break;
       } else {
         if constexpr (!streamed) {
-#pragma unroll
-          for (int c = 0; c < NOUTMAX / 16; ++c)
-            if (c * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + c * 16, r + 16 * c);
-          tc::tmem_wait_ld();
+          tc::tmem_load_n<NOUTMAX / 16>(lane_addr, r, (a.n_out_pad + 15) / 16);
         }
         last_ok = done;
       }

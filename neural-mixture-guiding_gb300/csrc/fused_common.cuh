@@ -335,8 +335,7 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     float v[16];
-    tc::tmem_ld16(lane_addr + 16 * g, v);
-    tc::tmem_wait_ld();
+    tc::tmem_load<1>(lane_addr + 16 * g, v);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       float lam, kap, nrm;
@@ -374,8 +373,7 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       float v[16];
-      tc::tmem_ld16(lane_addr + 16 * g, v);
-      tc::tmem_wait_ld();
+      tc::tmem_load<1>(lane_addr + 16 * g, v);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         float lam, kap, nrm;
@@ -394,8 +392,7 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
 #pragma unroll
   for (int g = 0; g < G; ++g) {
     float v[16];
-    tc::tmem_ld16(lane_addr + 16 * g, v);
-    tc::tmem_wait_ld();
+    tc::tmem_load<1>(lane_addr + 16 * g, v);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       float lam, kap, nrm;
@@ -409,8 +406,7 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
   float slogit = 0.f;
   if (a.sel && a.selection) {  // the selection logit follows the lobes (column 4K)
     float v[16];
-    tc::tmem_ld16(lane_addr + 4 * K, v);
-    tc::tmem_wait_ld();
+    tc::tmem_load<1>(lane_addr + 4 * K, v);
     slogit = v[0];
   }
   if (!valid) return;

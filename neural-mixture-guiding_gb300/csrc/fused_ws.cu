@@ -207,9 +207,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
         tc::fence_after_sync();
         if (!last) {
           float v[kWidth];
-#pragma unroll
-          for (int cc = 0; cc < kWidth / 16; ++cc) tc::tmem_ld16(lane_addr + cc * 16, v + 16 * cc);
-          tc::tmem_wait_ld();
+          tc::tmem_load<kWidth / 16>(lane_addr, v);
 #pragma unroll
           for (int cc = 0; cc < kWidth / 8; ++cc) store_chunk_relu(H, t, cc, kWidth / 8, v + 8 * cc, layer_fp16(a, l + 1));
           tc::fence_proxy_async();
@@ -224,10 +222,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1) k_fused_query_ws(const __grid
           }
         } else {
           if constexpr (!STREAM) {
-#pragma unroll
-            for (int cc = 0; cc < NOUTMAX / 16; ++cc)
-              if (cc * 16 < a.n_out_pad) tc::tmem_ld16(lane_addr + cc * 16, rr + 16 * cc);
-            tc::tmem_wait_ld();
+            tc::tmem_load_n<NOUTMAX / 16>(lane_addr, rr, (a.n_out_pad + 15) / 16);
             tc::fence_before_sync();
           }
           last_ok = d;
