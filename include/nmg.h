@@ -401,6 +401,32 @@ nmg_status nmg_extract_records(nmg_ctx* ctx, const nmg_radiance_records* records
                                int capacity, float* x, float* out_records, int* d_count, nmg_stream stream);
 
 /*
+ * One frame's training on its radiance records, as the reference's trainStep
+ * (integrator.cpp:650-701) does it: the records the rule of
+ * nmg_extract_records keeps are compacted into vertex_ids[capacity] (one
+ * 32-bit id per record, depth * image pixels + pixel; *d_count receives their
+ * number N, records beyond capacity are counted but not stored), then up to
+ * max_batches training steps run on consecutive batches of batch_size
+ * records: batch i holds min(N - i * batch_size, batch_size) records rounded
+ * down to a multiple of 128, and the batches stop at the first one below
+ * min_batch (the reference's MIN_TRAIN_BATCH_SIZE; it also caps the batches
+ * at batchPerFrame). N and the batch sizes are read on the device, so the call
+ * needs no host synchronisation; a batch with no records takes no optimiser
+ * step. On the fused paths the training kernel's load stage computes each
+ * record's network input row and GuidedOutput from the radiance-record arrays
+ * itself (the record rows never pass through HBM); the plain FP32 path
+ * gathers each batch's rows first. batch_size must be a multiple of 128 and
+ * at most the reserved batch. stats (may be NULL): [max_batches][2] FP64
+ * {mean loss, gradient norm}, zeros for batches not run.
+ * Replaces: GuidedPathTracer::trainStep (integrator.cpp:650-701):
+ * generate_training_data, the host read of the buffer size and the loop of
+ * network forward, compute_dL_doutput_divergence, backward and optimizer_step.
+ */
+nmg_status nmg_train_frame(nmg_ctx* ctx, const nmg_radiance_records* records, const nmg_train_pixels* pixels,
+                           int capacity, uint32_t* vertex_ids, int* d_count, int batch_size, int max_batches,
+                           int min_batch, double* stats, nmg_stream stream);
+
+/*
  * One frame's bounce loop as a CUDA graph. Bounce i runs the guided query of
  * its queue (device SoA `in`, uniforms u4, queue length *d_count read on the
  * device, at most n_max; d_count NULL = n_max) and then, when train_x is

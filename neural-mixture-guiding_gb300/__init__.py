@@ -208,6 +208,8 @@ def _bind_field(L):
         "nmg_save": [P, C.c_char_p],
         "nmg_export_tcnn": [P, C.c_char_p, C.c_int],
         "nmg_extract_records": [P, C.POINTER(RadianceRecords), C.POINTER(TrainPixels), C.c_int, P, P, P, P],
+        "nmg_train_frame": [P, C.POINTER(RadianceRecords), C.POINTER(TrainPixels), C.c_int, P, P, C.c_int, C.c_int,
+                            C.c_int, P, P],
         "nmg_import_tcnn": [P, C.c_char_p, P],
         "nmg_load": [P, C.c_char_p],
     }
@@ -482,13 +484,8 @@ class GuidingField:
         check_errors() raises NMGError with NMG_ERR_TIMEOUT."""
         check(self.L.nmg_selftest_wait_timeout(self.h, _stream(stream)))
 
-    def extract_records(self, records, cur_depth, offset, stride, train_res, res, capacity, product=True,
-                        stream=None, outputs=None):
-        """nmg_extract_records: records = list (one per depth) of dicts of device tensors (L, thp, pos, dir,
-        wi_pdf, bsdf_pdf, mis_weight, delta (uint8), bsdf_val, wo, normal, roughness). Returns
-        (x [capacity, n_input], records [capacity, record_floats], count (device int32 [1])); `outputs`
-        = such a triple to write into instead."""
-        import torch
+    @staticmethod
+    def _records(records, cur_depth, offset, stride, train_res, res, product):
         r = RadianceRecords()
         r.max_depth = len(records)
         r.product = int(product)
@@ -499,6 +496,16 @@ class GuidingField:
                 setattr(r.depth[d], name, t.data_ptr() if t is not None else None)
         tp = TrainPixels((C.c_uint * 2)(*offset), (C.c_uint * 2)(*stride), (C.c_uint * 2)(*train_res),
                          (C.c_uint * 2)(*res))
+        return r, tp
+
+    def extract_records(self, records, cur_depth, offset, stride, train_res, res, capacity, product=True,
+                        stream=None, outputs=None):
+        """nmg_extract_records: records = list (one per depth) of dicts of device tensors (L, thp, pos, dir,
+        wi_pdf, bsdf_pdf, mis_weight, delta (uint8), bsdf_val, wo, normal, roughness). Returns
+        (x [capacity, n_input], records [capacity, record_floats], count (device int32 [1])); `outputs`
+        = such a triple to write into instead."""
+        import torch
+        r, tp = self._records(records, cur_depth, offset, stride, train_res, res, product)
         if outputs is not None:
             x, rec, cnt = outputs  # nmg_extract_records resets the count itself
         else:
@@ -508,6 +515,24 @@ class GuidingField:
         check(self.L.nmg_extract_records(self.h, C.byref(r), C.byref(tp), int(capacity), _ptr(x), _ptr(rec),
                                          _ptr(cnt), _stream(stream)))
         return x, rec, cnt
+
+    def train_frame(self, records, cur_depth, offset, stride, train_res, res, capacity, batch_size, max_batches,
+                    min_batch, product=True, stream=None, outputs=None):
+        """nmg_train_frame: one frame's training on its radiance records (arguments as extract_records).
+        Returns (vertex ids (device int32 [capacity], the uint32 ids), count (device int32 [1]), stats
+        (device float64 [max_batches, 2]))."""
+        import torch
+        r, tp = self._records(records, cur_depth, offset, stride, train_res, res, product)
+        if outputs is not None:
+            ids, cnt, stats = outputs
+        else:
+            ids = torch.zeros(max(int(capacity), 1), dtype=torch.int32, device="cuda")
+            cnt = torch.zeros(1, dtype=torch.int32, device="cuda")
+            stats = torch.zeros((max_batches, 2), dtype=torch.float64, device="cuda")
+        check(self.L.nmg_train_frame(self.h, C.byref(r), C.byref(tp), int(capacity), _ptr(ids), _ptr(cnt),
+                                     int(batch_size), int(max_batches), int(min_batch), _ptr(stats),
+                                     _stream(stream)))
+        return ids, cnt, stats
 
     def export_tcnn(self, path, params_type="__half"):
         """Inference parameters as a tiny-cuda-nn Trainer snapshot (MessagePack)."""

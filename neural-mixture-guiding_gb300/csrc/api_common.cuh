@@ -70,6 +70,12 @@ inline int sm_count() {
     if (!(cond)) return nmg::set_error(NMG_ERR_INVALID_ARG, __VA_ARGS__); \
   } while (0)
 
+#define NMG_TRY(x)               \
+  do {                           \
+    nmg_status s_ = (x);         \
+    if (s_ != NMG_OK) return s_; \
+  } while (0)
+
 #define NMG_CUDA_TRY(call)                                                                 \
   do {                                                                                     \
     cudaError_t e_ = (call);                                                               \

@@ -33,6 +33,8 @@ struct Workspace {
   float* dh[2] = {};       // [cap_b][max(64, n_enc_pad)] ping-pong deltas
   double* partials = nullptr;  // block partial sums (loss, grad norm)
   int n_partials = 0;
+  int* batch_counts = nullptr; // [kMaxFrameBatches] record counts of nmg_train_frame's batches
+  float* recs = nullptr;       // [cap_b][8] GuidedOutput rows of a batch (plain path of nmg_train_frame)
   // fused path: host-side state object and its device allocation
   void* fused = nullptr;
   void* fused_dev = nullptr;
@@ -101,6 +103,17 @@ nmg_status fused_autotune(nmg_ctx* c, const nmg_shading* in, const float* u4, in
                           int use_cache, int* chosen, cudaStream_t st);
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st);
+// A training batch read from the frame's radiance records: row q is the path
+// vertex vid[id_base + q] (vertex id = depth * pixels + pixel).
+struct TrainRecords {
+  const uint32_t* vid;
+  long id_base;
+  uint32_t pixels;
+  const nmg_radiance_records* rr;
+};
+constexpr int kMaxFrameBatches = 64;
+nmg_status fused_train_step_src(nmg_ctx* c, const float* x, const float* rec, const TrainRecords* src,
+                                const int* d_count, int n_max, double* stats, cudaStream_t st);
 int fused_default_tiling(const nmg_ctx* c);
 
 // host_io.cu

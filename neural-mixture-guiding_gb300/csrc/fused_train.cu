@@ -38,6 +38,7 @@
 
 #include "api_common.cuh"
 #include "fused_common.cuh"
+#include "records.cuh"
 
 namespace nmg {
 
@@ -53,6 +54,14 @@ struct TrainArgs {
   long n_mlp;
   long layer_elem_off[kMaxLayers];  // element offset of each weight matrix in the parameter vector
   double* partials;     // [gridDim.x] loss partial sums
+  // Records mode (the kernel's REC instantiation): row q of the batch is the
+  // path vertex vid[id_base + q] of the frame's radiance records rr (vertex
+  // id = depth * pixels + pixel); the load stage computes its network input
+  // and GuidedOutput (vertex_record) instead of reading x and rec.
+  const uint32_t* vid;
+  long id_base;
+  uint32_t pixels;
+  nmg_radiance_records rr;
 };
 
 template <int K, int NOUTMAX>
@@ -172,7 +181,8 @@ constexpr int kScatRegLaunch = 128, kScatRegCompute = 168, kScatRegScatter = 88;
 static_assert(2 * kRows * kScatRegCompute + 2 * kRows * kScatRegScatter == 4 * kRows * kScatRegLaunch,
               "register split must equal the launch allocation");
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT,
+          bool REC>
 __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
     k_fused_train(const __grid_constant__ TrainArgs ta) {
   static_assert(!SCAT || NWG == 2, "scatter warps pair with two compute warpgroups");
@@ -183,7 +193,11 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   constexpr uint32_t A_BYTES = kRows * NENC * 2;
   constexpr uint32_t H_BYTES = kRows * kWidth * 2;
   constexpr uint32_t D_BYTES = kRows * DMAX * 2;
-  constexpr uint32_t WG_BYTES = A_BYTES + 3 * H_BYTES + D_BYTES;
+  // per warpgroup, after its operand tiles: each row's GuidedOutput (records
+  // mode REC: computed at the load stage, read at the loss stage) and, by
+  // tile parity, each row's normalised position for the scatter warps
+  constexpr uint32_t REC_BYTES = REC ? kRows * 8 * 4 : 0, P3_BYTES = SCAT ? 2 * kRows * 4 * 4 : 0;
+  constexpr uint32_t WG_BYTES = A_BYTES + 3 * H_BYTES + D_BYTES + REC_BYTES + P3_BYTES;
   constexpr int NL = 4;  // three hidden layers
   // TMEM: one forward/data-gradient accumulator per warpgroup, then the shared
   // weight-gradient accumulators (M = 64) dW0 | dW1 | dW2 | dW3^T.
@@ -204,6 +218,8 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   uint8_t* A0 = smem + w_region + g * WG_BYTES;
   uint8_t* Hs = A0 + A_BYTES;  // three hidden tiles
   uint8_t* Dt = Hs + 3 * H_BYTES;
+  float* s_rec = reinterpret_cast<float*>(Dt + D_BYTES);             // [kRows][8]
+  float* s_p3 = reinterpret_cast<float*>(Dt + D_BYTES + REC_BYTES);  // [2][kRows][4]
   // [0] weights, then ready[], done[], sfull[], sempty[]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * WG_BYTES);
   uint64_t* ready = bars + 1;
@@ -256,7 +272,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
     if (lane == 0 && ok) {
       int remaining[NWG], step[NWG];
       uint32_t rph[NWG];
-      bool first[4] = {true, true, true, true};
+      uint32_t started = 0;  // bit l: layer l's weight-gradient accumulator holds a sum
       bool any = false;
       for (int i = 0; i < NWG; ++i) {
         remaining[i] = 8 * wg_tiles(ntiles, i, NWG);
@@ -290,12 +306,13 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
             const int dwidth = l == NL - 1 ? nout : kWidth;
             const int in_w = l == 0 ? NENC : kWidth;
             const uint8_t* hin = l == 0 ? gA0 : gH + (l - 1) * H_BYTES;
+            const bool acc = (started >> l) & 1u;
             if (l == NL - 1)
-              issue_wgrad(tbase + CW3, tc::smem_u32(hin), kWidth / 8, tc::smem_u32(gD), dchunks, dwidth, fp16, !first[l]);
+              issue_wgrad(tbase + CW3, tc::smem_u32(hin), kWidth / 8, tc::smem_u32(gD), dchunks, dwidth, fp16, acc);
             else
               issue_wgrad(tbase + (l == 0 ? CW0 : (l == 1 ? CW1 : CW2)), tc::smem_u32(gD), dchunks, tc::smem_u32(hin),
-                          in_w / 8, in_w, fp16, !first[l]);
-            first[l] = false;
+                          in_w / 8, in_w, fp16, acc);
+            started |= 1u << l;
             // data gradient delta_l W_l (W_l's image as an MN-major operand); for l = 0 only the grid columns
             const uint32_t wk = uint32_t(in_w / 8) * 128u;
             issue_mma_kmajor(tD, tc::smem_u32(gD), dchunks, w_addr + a.layer_off[l], wk, 128u, 2u * wk,
@@ -331,13 +348,15 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
           ok = false;
           break;
         }
-        const float* dgs = reinterpret_cast<const float*>(smem + w_region + gg * WG_BYTES + A_BYTES + 2 * H_BYTES);
+        const uint8_t* gbase = smem + w_region + gg * WG_BYTES;
+        const float* dgs = reinterpret_cast<const float*>(gbase + A_BYTES + 2 * H_BYTES);
+        const float* gp3 = reinterpret_cast<const float*>(gbase + A_BYTES + 3 * H_BYTES + D_BYTES + REC_BYTES) +
+                           (k & 1) * kRows * 4;
         for (int item = sidx; item < kRows * LEVELS; item += kScatThreads) {
           const int r = item % kRows, lv = item / kRows;
           const long q = long(tile) * kRows + r;
           if (q < n) {
-            const float* xr = ta.x + q * a.enc.n_input;
-            const float p3[3] = {xr[0], xr[1], xr[2]};
+            const float p3[3] = {gp3[4 * r], gp3[4 * r + 1], gp3[4 * r + 2]};
             float df[F];
 #pragma unroll
             for (int kk = 0; kk < F; ++kk) df[kk] = dgs[(F * lv + kk) * kRows + r];
@@ -362,7 +381,25 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
       float x[10];
 #pragma unroll
       for (int d = 0; d < 10; ++d) x[d] = 0.f;
-      if (valid) load_row(ta.x, q, a.enc.n_input, x);
+      if (valid) {
+        if constexpr (REC) {
+          // records mode: the vertex's network input and GuidedOutput from the radiance records
+          const uint32_t v = ta.vid[ta.id_base + q];
+          const uint32_t dd = v / ta.pixels;
+          float out[7];
+          vertex_record(ta.rr.depth[dd], ta.rr.product, a.enc, v - dd * ta.pixels, x, out);
+#pragma unroll
+          for (int j = 0; j < 7; ++j) s_rec[t * 8 + j] = out[j];
+        } else {
+          load_row(ta.x, q, a.enc.n_input, x);
+        }
+      }
+      if constexpr (SCAT) {  // the scatter warps read this tile's positions from here (buffer kt & 1)
+        float* p3 = s_p3 + (kt & 1) * kRows * 4 + t * 4;
+        p3[0] = x[0];
+        p3[1] = x[1];
+        p3[2] = x[2];
+      }
       encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, false>(a, x, A0, t);
       ok = signal_ready(g, t, &ready[g], ok);
       if (!ok) break;
@@ -377,9 +414,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
         tc::fence_after_sync();
         if (l < NL - 1) {
           float v[kWidth];
-#pragma unroll
-          for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, v + 16 * c);
-          tc::tmem_wait_ld();
+          tc::tmem_load<kWidth / 16>(tD + lane_addr, v);
           uint8_t* H = Hs + l * H_BYTES;
           bool free_h = true;
           if (SCAT && l == 2 && kt > 0)  // the scatter warps still read the previous tile's gradient here
@@ -389,10 +424,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
           ok = signal_ready(g, t, &ready[g], fin && free_h && ok);
           if (!ok) break;
         } else {
-#pragma unroll
-          for (int c = 0; c < NOUTMAX / 16; ++c)
-            if (c * 16 < nout) tc::tmem_ld16(tD + lane_addr + c * 16, r + 16 * c);
-          tc::tmem_wait_ld();
+          tc::tmem_load_n<NOUTMAX / 16>(tD + lane_addr, r, (nout + 15) / 16);
           ok = fin && ok;
         }
       }
@@ -408,8 +440,13 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
         for (int i = 0; i < NOUTMAX; ++i) gr[i] = 0.f;
         if (valid) {
           float rr[8];
+          if constexpr (REC) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) rr[j] = j < ta.rstride ? ta.rec[q * ta.rstride + j] : 0.f;
+            for (int j = 0; j < 8; ++j) rr[j] = j < 7 ? s_rec[t * 8 + j] : 0.f;
+          } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) rr[j] = j < ta.rstride ? ta.rec[q * ta.rstride + j] : 0.f;
+          }
           loss_acc += double(tile_loss<K, NOUTMAX>(ta, r, rr, scale, gr));
         }
 #pragma unroll
@@ -431,9 +468,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
         dph ^= 1u;
         tc::fence_after_sync();
         float v[kWidth];
-#pragma unroll
-        for (int c = 0; c < kWidth / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, v + 16 * c);
-        tc::tmem_wait_ld();
+        tc::tmem_load<kWidth / 16>(tD + lane_addr, v);
         const uint8_t* H = Hs + (l - 1) * H_BYTES;
 #pragma unroll
         for (int c = 0; c < kWidth / 8; ++c) {
@@ -453,9 +488,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
         dph ^= 1u;
         tc::fence_after_sync();
         float dg[NGRID];
-#pragma unroll
-        for (int c = 0; c < NGRID / 16; ++c) tc::tmem_ld16(tD + lane_addr + c * 16, dg + 16 * c);
-        tc::tmem_wait_ld();
+        tc::tmem_load<NGRID / 16>(tD + lane_addr, dg);
         ok = bar_red_and(1 + g, kRows, fin && ok);
         if (!ok) break;
         if constexpr (SCAT) {
@@ -498,21 +531,27 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   if (ok && cta_tiles > 0 && !issuer && !scatter) {
     const int row = (warp & 3) * 16 + lane;  // valid for lane < 16
     const uint32_t qaddr = uint32_t((warp & 3) * 32) << 16;
-    const uint32_t cols[4] = {CW0, CW1, CW2, CW3};
-    const int widths[4] = {NENC, kWidth, kWidth, kWidth};
-    for (int m = g; m < 4; m += NWG) {
-      const int ncols = m == 3 ? nout : widths[m];
+    // one accumulator per layer m, warpgroup m % NWG flushing it; the layer's
+    // TMEM column and width are compile-time constants (no runtime-indexed
+    // local arrays: a build that held them on the stack read every layer from
+    // column 0)
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+      if (m % NWG != g) continue;
+      const uint32_t col_m = m == 0 ? CW0 : (m == 1 ? CW1 : (m == 2 ? CW2 : CW3));
+      const int width_m = m == 0 ? NENC : kWidth;
+      const int ncols = m == 3 ? nout : width_m;
+      const long off_m = ta.layer_elem_off[m];
       for (int c0 = 0; c0 < ncols; c0 += 16) {
         float v[16];
-        tc::tmem_ld16(tbase + qaddr + cols[m] + c0, v);
-        tc::tmem_wait_ld();
+        tc::tmem_load<1>(tbase + qaddr + col_m + uint32_t(c0), v);
         if (lane < 16) {
 #pragma unroll
           for (int i = 0; i < 16; ++i) {
             const int col = c0 + i;
             if (col >= ncols) continue;
-            const long idx = m < 3 ? ta.layer_elem_off[m] + long(row) * widths[m] + col  // dW_m[out = row][in = col]
-                                   : ta.layer_elem_off[3] + long(col) * kWidth + row;   // W3[out = col][in = row]
+            const long idx = m < 3 ? off_m + long(row) * width_m + col  // dW_m[out = row][in = col]
+                                   : off_m + long(col) * kWidth + row;  // W3[out = col][in = row]
             atomicAdd(ta.grad + idx, v[i] * inv_S);
           }
         }
@@ -542,12 +581,13 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   }
 }
 
-template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT>
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT,
+          bool REC>
 static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
   constexpr int DW = NOUTMAX > kWidth ? NOUTMAX : kWidth;
-  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, SCAT>;
+  auto kern = k_fused_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, SCAT, REC>;
   if constexpr (SCAT) {
     // the register split assumes the kernel was compiled to exactly its launch registers
     static int regs_ok = 0;
@@ -558,10 +598,12 @@ static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
                     ? 1
                     : -1;
     }
-    if (regs_ok < 0) return launch_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, false>(a, grid, st);
+    if (regs_ok < 0) return launch_train<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, NWG, false, REC>(a, grid, st);
   }
   const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) +
-                      NWG * (size_t(kRows) * NENC * 2 + 3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2) + 256;
+                      NWG * (size_t(kRows) * NENC * 2 + 3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2 +
+                             (REC ? size_t(kRows) * 8 * 4 : 0) + (SCAT ? 2 * size_t(kRows) * 4 * 4 : 0)) +
+                      256;
   nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
   if (s != NMG_OK) return s;
   kern<<<grid, SCAT ? 4 * kRows : NWG * kRows + 32, smem, st>>>(a);
@@ -570,6 +612,11 @@ static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
 
 nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const int* d_count, int n_max,
                             double* stats, cudaStream_t st) {
+  return fused_train_step_src(c, x, rec, nullptr, d_count, n_max, stats, st);
+}
+
+nmg_status fused_train_step_src(nmg_ctx* c, const float* x, const float* rec, const TrainRecords* src,
+                                const int* d_count, int n_max, double* stats, cudaStream_t st) {
   FusedState* s = fstate(c);
   if (!s) return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
   if (c->lay.n_layers != 4) return set_error(NMG_ERR_UNSUPPORTED, "fused training needs 3 hidden layers");
@@ -580,6 +627,12 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   a.f.n_max = n_max;
   a.x = x;
   a.rec = rec;
+  if (src) {
+    a.vid = src->vid;
+    a.id_base = src->id_base;
+    a.pixels = src->pixels;
+    a.rr = *src->rr;
+  }
   a.rstride = c->lay.record_floats;
   a.loss_scale = c->cfg.loss_scale;
   a.grad = c->grad;
@@ -595,10 +648,22 @@ nmg_status fused_train_step(nmg_ctx* c, const float* x, const float* rec, const 
   NMG_CUDA_TRY(cudaMemsetAsync(c->grad, 0, sizeof(float) * size_t(c->lay.n_params), st));
   NMG_CUDA_TRY(cudaMemsetAsync(c->ws.partials, 0, sizeof(double) * (c->ws.n_partials / 2), st));
   nmg_status r;
+  // the records mode is its own instantiation: the load stage of the plain
+  // one stays free of the record code
+  const bool recs = src != nullptr;
   switch (s->preset) {
-    case 1: r = launch_train<2, 16, 1, 4, 4, 8, 48, false, 2, true>(a, grid, st); break;
-    case 2: r = launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false>(a, grid, st); break;
-    case 3: r = launch_train<4, 8, 0, 2, 4, 8, 48, true, 2, true>(a, grid, st); break;
+    case 1:
+      r = recs ? launch_train<2, 16, 1, 4, 4, 8, 48, false, 2, true, true>(a, grid, st)
+               : launch_train<2, 16, 1, 4, 4, 8, 48, false, 2, true, false>(a, grid, st);
+      break;
+    case 2:
+      r = recs ? launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false, true>(a, grid, st)
+               : launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false, false>(a, grid, st);
+      break;
+    case 3:
+      r = recs ? launch_train<4, 8, 0, 2, 4, 8, 48, true, 2, true, true>(a, grid, st)
+               : launch_train<4, 8, 0, 2, 4, 8, 48, true, 2, true, false>(a, grid, st);
+      break;
     default: return set_error(NMG_ERR_UNSUPPORTED, "configuration has no fused kernel");
   }
   if (r != NMG_OK) return r;

@@ -145,6 +145,8 @@ static void free_workspace(nmg_ctx* c) {
   cudaFree(w.dh[0]);
   cudaFree(w.dh[1]);
   cudaFree(w.partials);
+  cudaFree(w.batch_counts);
+  cudaFree(w.recs);
   w = Workspace();
 }
 
@@ -170,6 +172,7 @@ static nmg_status reserve(nmg_ctx* c, int max_q, int max_b) {
   } while (0)
   A(w.x, capz * c->enc.n_input);
   A(w.partials, 2 * 2048);
+  A(w.batch_counts, kMaxFrameBatches);
   A(w.raw, capz * L.n_out_pad);
   w.n_partials = 2 * 2048;
   if (fp32) {
@@ -179,6 +182,7 @@ static nmg_status reserve(nmg_ctx* c, int max_q, int max_b) {
     if (max_b > 0) {
       const size_t wd = size_t(c->enc.n_enc_pad > kWidth ? c->enc.n_enc_pad : kWidth);
       A(w.draw, size_t(max_b) * L.n_out_pad);
+      A(w.recs, size_t(max_b) * 8);
       A(w.dh[0], size_t(max_b) * wd);
       A(w.dh[1], size_t(max_b) * wd);
     }

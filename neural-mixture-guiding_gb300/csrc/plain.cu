@@ -280,7 +280,14 @@ __global__ void k_grid_backward(EncodingParams e, const float* __restrict__ x, c
 }
 
 // ---------------------------------------------------------------- optimiser
-__global__ void k_step_inc(uint32_t* step) { *step += 1; }
+// A training step whose device count is zero takes no optimiser step (the
+// reference's training loop stops before a batch below its minimum size,
+// integrator.cpp:670-671): the step counter, Adam and the EMA leave the
+// parameters and the optimiser state as they are.
+__global__ void k_step_inc(uint32_t* step, const int* d_count) {
+  if (d_count && *d_count <= 0) return;
+  *step += 1;
+}
 
 // adam.h:47-119 + ema.h:62-75/102-145 in one pass over four parameters per
 // thread (128-bit loads and stores); also writes the reduced-precision copies
@@ -309,7 +316,8 @@ __global__ void __launch_bounds__(256) k_adam_ema(AdamArgs a, const float4* __re
                                                   float4* __restrict__ m, float4* __restrict__ v,
                                                   uint4* __restrict__ psteps, float4* __restrict__ w_inf,
                                                   uint2* __restrict__ w16, uint2* __restrict__ w16_inf,
-                                                  double* __restrict__ partials) {
+                                                  double* __restrict__ partials, const int* __restrict__ d_count) {
+  if (d_count && *d_count <= 0) return;  // an empty batch takes no step (see k_step_inc)
   const uint32_t step = *d_step;
   const float debias_old = 1.f - exp2f(float(step - 1) * a.log2_decay);
   const float debias_new = 1.f / (1.f - exp2f(float(step) * a.log2_decay));
@@ -388,9 +396,9 @@ __global__ void __launch_bounds__(kStatsThreads) k_finish_stats(const double* __
   for (int i = threadIdx.x; i < ng; i += kStatsThreads) b += gp[i];
   double sa = block_sum(a);
   double sb = block_sum(b);
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0) {  // an empty batch ran no Adam pass: its gradient-norm partials are stale
     stats[0] = n > 0 ? sa / double(n) : 0.0;
-    stats[1] = sqrt(sb);
+    stats[1] = n > 0 ? sqrt(sb) : 0.0;
   }
 }
 
@@ -447,12 +455,6 @@ static nmg_status launch_wgrad(const float* D, int ldd, int nout, const float* X
   k_linear_wgrad<<<blocks, threads, 0, st>>>(D, ldd, nout, X, ldx, nin, dW, d_count, n_max, rows_per_block);
   return check_launch("k_linear_wgrad");
 }
-
-#define NMG_TRY(x)                 \
-  do {                             \
-    nmg_status s_ = (x);           \
-    if (s_ != NMG_OK) return s_;   \
-  } while (0)
 
 nmg_status plain_featurize(nmg_ctx* c, const nmg_shading* in, const int* d_count, int n_max, float* x,
                            cudaStream_t st) {
@@ -556,7 +558,7 @@ static nmg_status plain_backward(nmg_ctx* c, const float* x, const int* d_count,
 nmg_status optimizer_step(nmg_ctx* c, const int* d_count, int n_max, double* stats, cudaStream_t st) {
   const Layout& L = c->lay;
   const nmg_config& g = c->cfg;
-  k_step_inc<<<1, 1, 0, st>>>(c->d_step);
+  k_step_inc<<<1, 1, 0, st>>>(c->d_step, d_count);
   const int nb = 152 * 8;
   double* gp = c->ws.partials + c->ws.n_partials / 2;
   if (L.n_params % 4 || L.n_mlp % 4) return set_error(NMG_ERR_UNSUPPORTED, "parameter count not a multiple of 4");
@@ -580,12 +582,12 @@ nmg_status optimizer_step(nmg_ctx* c, const int* d_count, int n_max, double* sta
                                          reinterpret_cast<float4*>(c->w), reinterpret_cast<float4*>(c->m),
                                          reinterpret_cast<float4*>(c->v), reinterpret_cast<uint4*>(c->psteps),
                                          reinterpret_cast<float4*>(c->w_inf), reinterpret_cast<uint2*>(c->w16),
-                                         reinterpret_cast<uint2*>(c->w16_inf), gp);
+                                         reinterpret_cast<uint2*>(c->w16_inf), gp, d_count);
   else
     k_adam_ema<false><<<nb, 256, 0, st>>>(aa, reinterpret_cast<const float4*>(c->grad), c->d_step,
                                           reinterpret_cast<float4*>(c->w), reinterpret_cast<float4*>(c->m),
                                           reinterpret_cast<float4*>(c->v), reinterpret_cast<uint4*>(c->psteps),
-                                          reinterpret_cast<float4*>(c->w_inf), nullptr, nullptr, gp);
+                                          reinterpret_cast<float4*>(c->w_inf), nullptr, nullptr, gp, d_count);
   NMG_TRY(check_launch("k_adam_ema"));
   if (stats) {
     k_finish_stats<<<1, kStatsThreads, 0, st>>>(c->ws.partials, c->ws.n_partials / 2, gp, nb, d_count, n_max,

@@ -1,28 +1,36 @@
 // records.cu -- training records from the per-pixel radiance records of a
-// frame (the reference's generate_training_data, train.cu:14-67).
+// frame (the reference's generate_training_data, train.cu:14-67), and one
+// frame's training on them (the reference's trainStep, integrator.cpp:650-701).
 //
 // The integrator stores, for every pixel and path vertex, the raw vertex data
 // (GuidedPixelStateBuffer::incrementDepth, workqueue.h:26-54) and adds the
 // radiance arriving later to every earlier vertex (recordRadiance,
 // workqueue.h:58-67). Once per frame a grid of training pixels (offset +
 // stride over the image) turns each non-delta vertex into one GuidedInput /
-// GuidedOutput pair: the local incident radiance L / thp (channels with
-// thp > 1e-5) weighted by the MIS weight (and by the BSDF value with product
-// sampling), its direction and pdfs, and the network inputs of the vertex.
-// A record is dropped, as in train.cu:57-62, when its normalised position,
-// its direction, its warped outgoing direction, its pdf or its local radiance
-// (tested BEFORE the BSDF factor, which multiplies only the stored copy) has
-// a NaN, or its pdf is zero; a NaN BSDF value alone keeps the record, with a
-// NaN radiance, as it does in the reference. Here one thread per training
-// pixel walks its vertices and appends
-// the records with one atomic per block and vertex depth (block-aggregated:
-// the append counter is a single address, and one atomic per warp and depth
-// serialised on it: 715 -> 530 us for a 1920x1080 frame of 6 bounces), so the
-// count can feed nmg_train_step's device count directly. (Counting every
-// vertex first for one atomic per block and round, then writing, measured
-// 800 us: the second pass over the vertices costs more than it saves.)
+// GuidedOutput pair (vertex_record, records.cuh): the local incident radiance
+// L / thp (channels with thp > 1e-5) weighted by the MIS weight (and by the
+// BSDF value with product sampling), its direction and pdfs, and the network
+// inputs of the vertex. A record is dropped, as in train.cu:57-62, when its
+// normalised position, its direction, its warped outgoing direction, its pdf
+// or its local radiance (tested BEFORE the BSDF factor, which multiplies only
+// the stored copy) has a NaN, or its pdf is zero; a NaN BSDF value alone keeps
+// the record, with a NaN radiance, as it does in the reference.
+//
+// The extraction kernel runs one block per (group of 256 training pixels,
+// depth), so that the vertices of different depths load in parallel, and
+// appends with one atomic per block and round (block-aggregated: the append
+// counter is a single address; one atomic per warp serialised on it), staging
+// the block's rows in shared memory so that they leave as contiguous stores.
+// The count stays on the device and can feed nmg_train_step directly.
+// Measured for a 1920x1080 frame of 6 bounces: 715 us with one atomic per
+// warp, 530 us per block, 495 us with the staged stores, 365 us once every
+// field of a vertex is loaded before any is tested. (Counting every vertex
+// first, then writing, measured 800 us: the second pass over the vertices
+// costs more than it saves.)
+#include <string.h>
+
 #include "api_common.cuh"
-#include "ctx.cuh"
+#include "records.cuh"
 
 namespace nmg {
 
@@ -34,135 +42,124 @@ struct RecordArgs {
   int capacity;
   float* x;
   float* rec;
+  uint32_t* ids;
   int* count;
 };
 
 constexpr int kRecordThreads = 256;
 
+// blockIdx.y is the depth. IDS: write 32-bit vertex ids instead of rows.
+template <bool IDS>
 __global__ void __launch_bounds__(kRecordThreads) k_extract_records(const __grid_constant__ RecordArgs a) {
-  __shared__ int s_warp[2][kRecordThreads / 32];  // per warp: its count, then its offset (by depth parity)
-  __shared__ int s_base[2];                       // the block's first index for this depth
+  __shared__ int s_warp[2][kRecordThreads / 32];  // per warp: its count, then its offset (by round parity)
+  __shared__ int s_base[2];                       // the block's first index for this round
+  __shared__ int s_tot[2];                        // the block's record count for this round
+  // The block's rows of one round, compacted, so that they leave as contiguous
+  // coalesced stores (a thread storing its own 10- and 7-float rows would touch
+  // ~40 sectors per warp store for 4 bytes of each)
+  __shared__ float s_x[IDS ? 1 : kRecordThreads * 10], s_r[IDS ? 1 : kRecordThreads * 7];
+  __shared__ uint32_t s_id[IDS ? kRecordThreads : 1];
   const long n = long(a.tp.train_res[0]) * a.tp.train_res[1];
+  const uint32_t pixels = a.tp.res[0] * a.tp.res[1];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int ni = a.enc.n_input, rf = a.selection ? 7 : 6;
-  const int max_depth = a.r.max_depth < NMG_MAX_TRAIN_DEPTH ? a.r.max_depth : NMG_MAX_TRAIN_DEPTH;
+  const int d = blockIdx.y;
   // grid-stride over whole blocks, so that every thread reaches the block-wide barriers
-  for (long base = long(blockIdx.x) * blockDim.x; base < n; base += long(gridDim.x) * blockDim.x) {
+  int round = 0;
+  for (long base = long(blockIdx.x) * blockDim.x; base < n; base += long(gridDim.x) * blockDim.x, ++round) {
     const long tid = base + threadIdx.x;
-    int pixel = -1, depth = 0;
+    int pixel = -1;
     if (tid < n) {
       const uint32_t tx = uint32_t(tid % a.tp.train_res[0]), ty = uint32_t(tid / a.tp.train_res[0]);
       const uint32_t px = tx * a.tp.stride[0] + a.tp.offset[0], py = ty * a.tp.stride[1] + a.tp.offset[1];
-      if (px < a.tp.res[0] && py < a.tp.res[1]) {
-        pixel = int(px + py * a.tp.res[0]);
-        depth = int(a.r.cur_depth[pixel]);
-        depth = depth < max_depth ? depth : max_depth;
+      if (px < a.tp.res[0] && py < a.tp.res[1]) pixel = int(px + py * a.tp.res[0]);
+    }
+    bool keep = false;
+    float xin[10], out[7];
+    if (pixel >= 0 && d < int(a.r.cur_depth[pixel]))
+      keep = vertex_record(a.r.depth[d], a.r.product, a.enc, uint32_t(pixel), xin, out);
+    // block-aggregated append: the warps' counts, one atomic for the block, then each warp's offset.
+    // A warp's slot is rewritten only by its own lane 0, after the next __ballot_sync, which every
+    // lane of the warp reaches only after its reads; thread 0 rewrites the totals and the base only
+    // after the next round's first barrier; the slots also alternate with the round's parity.
+    const int sb = round & 1;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) s_warp[sb][warp] = __popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int tot = 0;
+      for (int w = 0; w < kRecordThreads / 32; ++w) {
+        const int c = s_warp[sb][w];
+        s_warp[sb][w] = tot;
+        tot += c;
+      }
+      s_base[sb] = tot ? atomicAdd(a.count, tot) : 0;
+      s_tot[sb] = tot;
+    }
+    __syncthreads();
+    if (keep) {
+      const int local = s_warp[sb][warp] + __popc(m & ((1u << lane) - 1u));
+      if constexpr (IDS) {
+        s_id[local] = vertex_id(d, uint32_t(pixel), pixels);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 10; ++k)
+          if (k < ni) s_x[local * ni + k] = xin[k];
+#pragma unroll
+        for (int k = 0; k < 7; ++k)
+          if (k < rf) s_r[local * rf + k] = out[k];
       }
     }
-    for (int d = 0; d < max_depth; ++d) {
-      bool keep = false;
-      float xin[10], out[7];
-      if (pixel >= 0 && d < depth) {
-        const auto& R = a.r.depth[d];
-        keep = !R.delta || !R.delta[pixel];
-        if (keep) {
-          const f3 pos = load3(R.pos, pixel);
-          const float th = R.dir[2 * pixel], ph = R.dir[2 * pixel + 1];
-          const float wi_pdf = R.wi_pdf[pixel];
-          const float mis = R.mis_weight[pixel];
-          // local radiance (train.cu:44-49): L / thp per channel with thp > 1e-5,
-          // times the MIS weight. The NaN test below reads this L; the BSDF value
-          // multiplies only the stored copy (train.cu:50-53), as in the reference.
-          float L[3], Lout[3];
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const float thp = R.thp[3 * pixel + c];
-            L[c] = thp > NMG_EPS ? __fdiv_rn(R.L[3 * pixel + c], thp) : 0.f;
-            L[c] = __fmul_rn(L[c], mis);
-            Lout[c] = (a.r.product && R.bsdf_val) ? __fmul_rn(L[c], R.bsdf_val[3 * pixel + c]) : L[c];
-          }
-          // network inputs (train.cu:34-43): the position in the inflated box,
-          // the outgoing direction and the auxiliary normal/roughness inputs
-          float sw, cw, sp, cp;
-          sincosf(R.wo[2 * pixel], &sw, &cw);
-          sincosf(R.wo[2 * pixel + 1], &sp, &cp);
-          const f3 wo{sw * cp, sw * sp, cw};
-          const float nth = R.normal[2 * pixel], nph = R.normal[2 * pixel + 1];
-          const float rough = R.roughness[pixel];
-          // normalizeSpatialCoord (train.h:173-177), bit for bit
-          const float p[3] = {pos.x, pos.y, pos.z};
-          const float infl = aabb_inflation(a.enc.aabb);
-          for (int k = 0; k < 3; ++k) xin[k] = normalize_coord(a.enc.aabb, infl, k, p[k]);
-          xin[3] = (wo.x + 1.f) * 0.5f;
-          xin[4] = (wo.y + 1.f) * 0.5f;
-          xin[5] = (wo.z + 1.f) * 0.5f;
-          if (a.enc.input_mode == 0) {
-            xin[6] = nth * NMG_INV_PI;
-            xin[7] = nph * NMG_INV_2PI;
-            xin[8] = 1.f - expf(-rough);
-          } else {
-            float sn, cn, sq, cq;
-            sincosf(nth, &sn, &cn);
-            sincosf(nph, &sq, &cq);
-            xin[6] = (sn * cq + 1.f) * 0.5f;
-            xin[7] = (sn * sq + 1.f) * 0.5f;
-            xin[8] = (cn + 1.f) * 0.5f;
-            xin[9] = 1.f - expf(-rough);
-          }
-          out[0] = th;
-          out[1] = ph;
-          out[2] = Lout[0];
-          out[3] = Lout[1];
-          out[4] = Lout[2];
-          out[5] = wi_pdf;
-          out[6] = R.bsdf_pdf ? R.bsdf_pdf[pixel] : 0.f;
-          // train.cu:57-62: NaN in the normalised position, the stored direction,
-          // the warped outgoing direction (the networks here always take wo as an
-          // input, as the reference's default product-sampling build does), the
-          // pdf or the local radiance before the BSDF factor, or a zero pdf
-          keep = !(isnan(xin[0]) || isnan(xin[1]) || isnan(xin[2]) || isnan(th) || isnan(ph) || isnan(xin[3]) ||
-                   isnan(xin[4]) || isnan(xin[5]) || isnan(wi_pdf) || wi_pdf == 0.f || isnan(L[0]) ||
-                   isnan(L[1]) || isnan(L[2]));
-        }
-      }
-      // block-aggregated append: the warps' counts, one atomic for the block, then each warp's offset
-      // (two barriers per depth). No barrier is needed after the offsets are read: a warp's slot is
-      // rewritten only by its own lane 0, after the next __ballot_sync, which every lane of the warp
-      // reaches only after its reads, and thread 0 rewrites the totals and the base only after the
-      // next depth's first barrier; the slots also alternate with the depth's parity.
-      const int sb = d & 1;
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (lane == 0) s_warp[sb][warp] = __popc(m);
-      __syncthreads();
-      if (threadIdx.x == 0) {
-        int tot = 0;
-        for (int w = 0; w < kRecordThreads / 32; ++w) {
-          const int c = s_warp[sb][w];
-          s_warp[sb][w] = tot;
-          tot += c;
-        }
-        s_base[sb] = tot ? atomicAdd(a.count, tot) : 0;
-      }
-      __syncthreads();
-      if (keep) {
-        const long idx = long(s_base[sb]) + s_warp[sb][warp] + __popc(m & ((1u << lane) - 1u));
-        if (idx < a.capacity) {
-          for (int k = 0; k < ni; ++k) a.x[idx * ni + k] = xin[k];
-          for (int k = 0; k < rf; ++k) a.rec[idx * rf + k] = out[k];
-        }
-      }
+    __syncthreads();
+    // the block's rows [base, base + tot), written out contiguously (up to the capacity); the staged rows
+    // are rewritten only after the next round's two barriers, which every thread reaches after this copy
+    const long rbase = s_base[sb];
+    const int tot = s_tot[sb];
+    const long rows = rbase + tot <= a.capacity ? tot : (rbase < a.capacity ? a.capacity - rbase : 0);
+    if constexpr (IDS) {
+      for (long i = threadIdx.x; i < rows; i += kRecordThreads) a.ids[rbase + i] = s_id[i];
+    } else {
+      for (long i = threadIdx.x; i < rows * ni; i += kRecordThreads) a.x[rbase * ni + i] = s_x[i];
+      for (long i = threadIdx.x; i < rows * rf; i += kRecordThreads) a.rec[rbase * rf + i] = s_r[i];
     }
   }
 }
 
-}  // namespace nmg
+// Record counts of a frame's training batches, as the reference's training
+// loop sizes them (integrator.cpp:666-672): batch i holds min(N - i B, B) of
+// the N stored records, rounded down to a multiple of 128, and the loop stops
+// at the first batch below min_batch (the sizes only shrink with i, so every
+// later batch is below it too). A count of 0 makes that batch's training step
+// a no-op (no optimiser step).
+__global__ void k_batch_counts(const int* __restrict__ d_count, int capacity, int batch, int batches, int min_batch,
+                               int* __restrict__ counts) {
+  int n = *d_count;
+  n = n < 0 ? 0 : (n > capacity ? capacity : n);
+  for (int i = threadIdx.x; i < batches; i += blockDim.x) {
+    const long rem = long(n) - long(i) * batch;
+    long c = rem < 0 ? 0 : (rem > batch ? batch : rem);
+    c -= c % 128;
+    counts[i] = (c > 0 && c >= min_batch) ? int(c) : 0;
+  }
+}
 
-using namespace nmg;
+// Rows of one batch for the plain path: x[q][n_input] and rec[q][rf] of the
+// vertices vid[base + q], q < *count.
+__global__ void k_gather_rows(nmg_radiance_records rr, EncodingParams enc, int rf, const uint32_t* __restrict__ vid,
+                              long base, uint32_t pixels, const int* __restrict__ count, int n_max,
+                              float* __restrict__ x, float* __restrict__ rec) {
+  int n = *count;
+  n = n > n_max ? n_max : n;
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += long(gridDim.x) * blockDim.x) {
+    const uint32_t v = vid[base + q], d = v / pixels;
+    float xin[10], out[7];
+    vertex_record(rr.depth[d], rr.product, enc, v - d * pixels, xin, out);
+    for (int k = 0; k < enc.n_input; ++k) x[q * enc.n_input + k] = xin[k];
+    for (int k = 0; k < rf; ++k) rec[q * rf + k] = out[k];
+  }
+}
 
-extern "C" nmg_status nmg_extract_records(nmg_ctx* c, const nmg_radiance_records* r, const nmg_train_pixels* tp,
-                                          int capacity, float* x, float* records, int* d_count, nmg_stream stream) {
-  NMG_REQUIRE(c && r && tp && x && records && d_count, "NULL argument");
-  NMG_REQUIRE(capacity >= 0, "capacity=%d", capacity);
+static nmg_status check_records(const nmg_ctx* c, const nmg_radiance_records* r, const nmg_train_pixels* tp) {
   NMG_REQUIRE(r->max_depth >= 0 && r->max_depth <= NMG_MAX_TRAIN_DEPTH, "max_depth=%d (0..%d)", r->max_depth,
               NMG_MAX_TRAIN_DEPTH);
   NMG_REQUIRE(tp->stride[0] >= 1 && tp->stride[1] >= 1, "zero training-pixel stride");
@@ -174,20 +171,92 @@ extern "C" nmg_status nmg_extract_records(nmg_ctx* c, const nmg_radiance_records
                 "NULL record array at depth %d", d);
     NMG_REQUIRE(!c->cfg.selection || R.bsdf_pdf, "learned selection needs bsdf_pdf (depth %d)", d);
   }
-  cudaStream_t st = (cudaStream_t)stream;
-  NMG_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(int), st));
-  if (n == 0 || r->max_depth == 0) return NMG_OK;
+  return NMG_OK;
+}
+
+static RecordArgs record_args(const nmg_ctx* c, const nmg_radiance_records* r, const nmg_train_pixels* tp,
+                              int capacity, int* d_count) {
   RecordArgs a;
+  memset(&a, 0, sizeof(a));
   a.r = *r;
   a.tp = *tp;
   a.enc = c->enc;
   a.selection = c->cfg.selection;
   a.capacity = capacity;
+  a.count = d_count;
+  return a;
+}
+
+// Blocks of the extraction grid along the pixels (the depths are its second
+// dimension): about 8 blocks per SM in all.
+static unsigned extraction_blocks(long n, int depths) {
+  const long blocks = (n + kRecordThreads - 1) / kRecordThreads;
+  const long cap = (152L * 8 + depths - 1) / depths;
+  return unsigned(blocks > cap ? cap : (blocks > 0 ? blocks : 1));
+}
+
+}  // namespace nmg
+
+using namespace nmg;
+
+extern "C" nmg_status nmg_extract_records(nmg_ctx* c, const nmg_radiance_records* r, const nmg_train_pixels* tp,
+                                          int capacity, float* x, float* records, int* d_count, nmg_stream stream) {
+  NMG_REQUIRE(c && r && tp && x && records && d_count, "NULL argument");
+  NMG_REQUIRE(capacity >= 0, "capacity=%d", capacity);
+  NMG_TRY(check_records(c, r, tp));
+  cudaStream_t st = (cudaStream_t)stream;
+  NMG_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(int), st));
+  const long n = long(tp->train_res[0]) * tp->train_res[1];
+  if (n == 0 || r->max_depth == 0) return NMG_OK;
+  RecordArgs a = record_args(c, r, tp, capacity, d_count);
   a.x = x;
   a.rec = records;
-  a.count = d_count;
-  long blocks = (n + kRecordThreads - 1) / kRecordThreads;
-  if (blocks > 152L * 8) blocks = 152L * 8;
-  k_extract_records<<<int(blocks), kRecordThreads, 0, st>>>(a);
+  const int depths = r->max_depth;
+  k_extract_records<false><<<dim3(extraction_blocks(n, depths), unsigned(depths)), kRecordThreads, 0, st>>>(a);
   return check_launch("k_extract_records");
+}
+
+extern "C" nmg_status nmg_train_frame(nmg_ctx* c, const nmg_radiance_records* r, const nmg_train_pixels* tp,
+                                      int capacity, uint32_t* vertex_ids, int* d_count, int batch_size,
+                                      int max_batches, int min_batch, double* stats, nmg_stream stream) {
+  NMG_REQUIRE(c && r && tp && vertex_ids && d_count, "NULL argument");
+  NMG_REQUIRE(capacity >= 0, "capacity=%d", capacity);
+  NMG_REQUIRE(batch_size > 0 && batch_size % 128 == 0, "batch_size=%d (a positive multiple of 128)", batch_size);
+  NMG_REQUIRE(max_batches >= 1 && max_batches <= kMaxFrameBatches, "max_batches=%d (1..%d)", max_batches,
+              kMaxFrameBatches);
+  NMG_REQUIRE(min_batch >= 0, "min_batch=%d", min_batch);
+  NMG_TRY(check_records(c, r, tp));
+  const uint64_t pixels = uint64_t(tp->res[0]) * tp->res[1];
+  NMG_REQUIRE(pixels * NMG_MAX_TRAIN_DEPTH < (1ull << 32), "image of %llu pixels: vertex ids need 32 bits",
+              (unsigned long long)pixels);
+  if (batch_size > c->ws.cap_b || !c->ws.batch_counts)
+    return set_error(NMG_ERR_CAPACITY, "batch %d above reserved %d (call nmg_reserve)", batch_size, c->ws.cap_b);
+  cudaStream_t st = (cudaStream_t)stream;
+  NMG_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(int), st));
+  if (stats) NMG_CUDA_TRY(cudaMemsetAsync(stats, 0, sizeof(double) * 2 * size_t(max_batches), st));
+  const long n = long(tp->train_res[0]) * tp->train_res[1];
+  if (n > 0 && r->max_depth > 0) {
+    RecordArgs a = record_args(c, r, tp, capacity, d_count);
+    a.ids = vertex_ids;
+    const int depths = r->max_depth;
+    k_extract_records<true><<<dim3(extraction_blocks(n, depths), unsigned(depths)), kRecordThreads, 0, st>>>(a);
+    NMG_TRY(check_launch("k_extract_records"));
+  }
+  k_batch_counts<<<1, kMaxFrameBatches, 0, st>>>(d_count, capacity, batch_size, max_batches, min_batch,
+                                                  c->ws.batch_counts);
+  NMG_TRY(check_launch("k_batch_counts"));
+  for (int i = 0; i < max_batches; ++i) {
+    const int* count = c->ws.batch_counts + i;
+    double* st_i = stats ? stats + 2 * i : nullptr;
+    if (c->cfg.path == NMG_PATH_FP32) {
+      k_gather_rows<<<152 * 4, 256, 0, st>>>(*r, c->enc, c->lay.record_floats, vertex_ids, long(i) * batch_size,
+                                             uint32_t(pixels), count, batch_size, c->ws.x, c->ws.recs);
+      NMG_TRY(check_launch("k_gather_rows"));
+      NMG_TRY(plain_train_step(c, c->ws.x, c->ws.recs, count, batch_size, st_i, st));
+    } else {
+      const TrainRecords src{vertex_ids, long(i) * batch_size, uint32_t(pixels), r};
+      NMG_TRY(fused_train_step_src(c, nullptr, nullptr, &src, count, batch_size, st_i, st));
+    }
+  }
+  return NMG_OK;
 }

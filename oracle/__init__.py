@@ -295,7 +295,7 @@ def ref_featurize_queue(pos, wo, normal, rough, aabb):
 
 
 def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_mode=0, product=True,
-                    selection=False):
+                    selection=False, return_vertex=False):
     """Training records from per-pixel radiance records, restating the
     reference's generate_training_data (src/render/guided/train.cu:14-67) with
     normalizeSpatialCoord (train.h:173-177) in FP32, one IEEE operation at a
@@ -312,7 +312,8 @@ def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_
     rec: dict of per-depth arrays [depth][pixels(, c)]: L, thp, pos, bsdf_val
     (3 channels), dir, wo, normal (2 angles), wi_pdf, bsdf_pdf, mis_weight,
     roughness, delta. Returns (x [n, 9|10], records [n, 6|7]) as float32 in
-    the reference's loop order (training pixel, then depth)."""
+    the reference's loop order (training pixel, then depth); with
+    return_vertex also the (pixel, depth) of every row [n, 2]."""
     f = np.float32
     aabb = np.asarray(aabb, np.float32)
     mn, mx = aabb[:3], aabb[3:]
@@ -323,7 +324,7 @@ def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_
     ctr = (lo + hi) / f(2)
     diag = hi - lo
     eps = f(1e-5)  # M_EPSILON (krrmath constants.h:25)
-    xs, outs = [], []
+    xs, outs, verts = [], [], []
     with np.errstate(invalid="ignore", divide="ignore", over="ignore"):
         for ty in range(train_res[1]):
             for tx in range(train_res[0]):
@@ -361,8 +362,13 @@ def extract_records(rec, cur_depth, offset, stride, train_res, res, aabb, input_
                     if selection:
                         o.append(f(rec["bsdf_pdf"][d][pid]))
                     outs.append(o)
+                    verts.append((pid, d))
     ni = 9 if input_mode == 0 else 10
-    return (np.array(xs, np.float32).reshape(-1, ni), np.array(outs, np.float32).reshape(-1, 7 if selection else 6))
+    x = np.array(xs, np.float32).reshape(-1, ni)
+    out = np.array(outs, np.float32).reshape(-1, 7 if selection else 6)
+    if return_vertex:
+        return x, out, np.array(verts, np.int64).reshape(-1, 2)
+    return x, out
 
 
 # ---------------------------------------------------------------------------
