@@ -269,6 +269,53 @@ NMG_D void encode_row(const FusedArgs& a, const float (&x)[10], uint8_t* tile, i
   for (int ch = 0; ch < (NPAD - NGRID) / 8; ++ch) store_chunk(tile, row, NGRID / 8 + ch, KC, d + 8 * ch, fp16);
 }
 
+// encode_row for one of the two threads that share a row: half h writes the
+// grid chunks ch with ch % 2 == h (each chunk 8 / F consecutive levels, so
+// both halves get coarse and fine levels) and its share of the direction
+// chunks: for input mode 1 half 0 the SH(wo) chunks and half 1 the rest
+// (SH(normal), one-blob(roughness), padding), each computing only what it
+// stores; for mode 0, whose encodings share chunks, both compute the whole
+// direction part and split its chunks. Together the two calls write exactly
+// what encode_row writes.
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, bool SMOOTH, bool PAIR = false>
+NMG_D void encode_row_half(const FusedArgs& a, const float (&x)[10], uint8_t* tile, int row, int h) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NGRID = LEVELS * F;
+  constexpr int NPAD = (NGRID + NDIR + 15) / 16 * 16;
+  constexpr int KC = NPAD / 8;
+  constexpr int LPC = 8 / F;
+  constexpr int GCH = NGRID / 8, DCH = (NPAD - NGRID) / 8;
+  constexpr bool SPLIT_SH = MODE == 1 && (SHDEG * SHDEG) % 8 == 0;
+  constexpr int DCH0 = SPLIT_SH ? SHDEG * SHDEG / 8 : (DCH + 1) / 2;  // direction chunks of half 0
+  static_assert(NGRID % 16 == 0, "grid chunks split evenly over the two halves");
+  const bool fp16 = a.fp16 != 0;
+  const float p3[3] = {x[0], x[1], x[2]};
+#pragma unroll 1
+  for (int ch = h; ch < GCH; ch += 2) {
+    float f[8];
+#pragma unroll
+    for (int j = 0; j < LPC; ++j) grid_level<F, SMOOTH, PAIR>(a, ch * LPC + j, p3, f + j * F);
+    store_chunk(tile, row, ch, KC, f, fp16);
+  }
+  float d[NPAD - NGRID];
+#pragma unroll
+  for (int k = 0; k < NPAD - NGRID; ++k) d[k] = 1.f;
+  if (MODE == 0) {
+    sh_basis(SHDEG, x[3] * 2.f - 1.f, x[4] * 2.f - 1.f, x[5] * 2.f - 1.f, d);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) oneblob_fixed<BINS>(x[6 + k], d + SHDEG * SHDEG + k * BINS);
+  } else if (!SPLIT_SH || h == 0) {
+    sh_basis(SHDEG, x[3] * 2.f - 1.f, x[4] * 2.f - 1.f, x[5] * 2.f - 1.f, d);
+  }
+  if (MODE == 1 && (!SPLIT_SH || h == 1)) {
+    sh_basis(SHDEG, x[6] * 2.f - 1.f, x[7] * 2.f - 1.f, x[8] * 2.f - 1.f, d + SHDEG * SHDEG);
+    oneblob_fixed<BINS>(x[9], d + 2 * SHDEG * SHDEG);
+  }
+#pragma unroll
+  for (int ch = 0; ch < DCH; ++ch)
+    if ((ch < DCH0) == (h == 0)) store_chunk(tile, row, GCH + ch, KC, d + 8 * ch, fp16);
+}
+
 // Loads network input row q (n_input <= 10 floats) with compile-time indices.
 NMG_D void load_row(const float* x, long q, int n_input, float (&v)[10]) {
 #pragma unroll

@@ -1,12 +1,16 @@
 // fused_train.cu -- the fused reduced-precision training step on tcgen05.
 //
-// One persistent CTA per SM: two compute warpgroups (128 threads each, one per
-// K = 16 configuration) walking tiles of 128 training records, plus one MMA
-// issuer warp. All tensor-core work of the CTA is issued by one thread of that
-// warp, in each warpgroup's order, so the shared weight-gradient accumulators
-// see their MMAs in sequence; a warpgroup signals "operands ready" on an
-// mbarrier and waits on its "done" mbarrier (tcgen05.commit). For each tile,
-// entirely on chip:
+// One persistent CTA per SM: two pipelines (one for the K = 16 configuration)
+// walking tiles of 128 training records, plus one MMA issuer warp. A pipeline
+// is two warpgroups, so every record has two threads: warps w and w + 4 read
+// the same TMEM lane quadrant, and each half of a row's pair takes half of
+// every phase -- half the grid levels of the encoding, half the columns of
+// each epilogue, half the mixture lobes of the loss (the two partial sums the
+// loss needs cross through shared memory). All tensor-core work of the CTA is
+// issued by one thread of the issuer warp, in each pipeline's order, so the
+// shared weight-gradient accumulators see their MMAs in sequence; a pipeline
+// signals "operands ready" on an mbarrier and waits on its "done" mbarrier
+// (tcgen05.commit). For each tile, entirely on chip:
 //   encode the input rows into a BF16/FP16 operand tile (A0)
 //   forward:  h0 = relu(A0 W0^T), h1, h2 (kept in shared memory), raw = h2 W3^T
 //   adjoint:  KL loss and dL/draw per record in registers (train.cu:69-124)
@@ -22,7 +26,7 @@
 // After the last tile each CTA adds its TMEM weight gradients into the
 // global gradient. Adam + EMA then run as one streaming kernel.
 //
-// TMEM (512 columns): one forward/data-gradient accumulator per warpgroup
+// TMEM (512 columns): one forward/data-gradient accumulator per pipeline
 // (M = 128; 64 columns, 128 when the output layer is wider), then the shared
 // weight-gradient accumulators dW0 | dW1 | dW2 | dW3^T (M = 64: rows live in
 // lanes 0-15 of each 32-lane subpartition). The layer-0 data gradient is
@@ -42,7 +46,7 @@
 
 namespace nmg {
 
-constexpr uint32_t kColD = 0, kColW0 = 128, kColW1 = 208, kColW2 = 272, kColW3 = 336, kTrainCols = 512;
+constexpr uint32_t kTrainCols = 512;
 
 struct TrainArgs {
   FusedArgs f;          // encoding, weights image (training weights), table
@@ -63,12 +67,6 @@ struct TrainArgs {
   uint32_t pixels;
   nmg_radiance_records rr;
 };
-
-template <int K, int NOUTMAX>
-NMG_D float tile_loss(const TrainArgs& a, const float (&r)[NOUTMAX], const float* rec, float scale, float* g) {
-  if (a.f.selection) return mix_kl_loss_grad_selection<K, true>(r, rec, scale, a.f.mix, g);
-  return mix_kl_loss_grad<K, true>(r, rec, scale, a.f.mix, g);
-}
 
 NMG_D void issue_mma_kmajor(uint32_t tmem, uint32_t a_addr, int a_chunks, uint32_t b_addr, uint32_t b_lbo,
                             uint32_t b_sbo, uint32_t b_step, int N, int ksteps, bool fp16, bool b_mn) {
@@ -114,15 +112,16 @@ NMG_D int wg_tiles(int ntiles, int g, int nwg) {
   return first < ntiles ? (ntiles - 1 - first) / stride + 1 : 0;
 }
 
-// Signals the issuer that this warpgroup's operands for its next MMA batch
-// are in shared memory (and that its last TMEM reads are done): every thread
-// makes its writes visible to the tensor core, the group synchronises (and
-// agrees on `ok`), and one thread arrives on the group's ready barrier.
-NMG_D bool signal_ready(int g, int t, uint64_t* ready, bool ok) {
+// Signals the issuer that pipeline g's operands for its next MMA batch are in
+// shared memory (and that its last TMEM reads are done): every thread makes
+// its writes visible to the tensor core, the pipeline's two warpgroups
+// synchronise (and agree on `ok`), and one thread arrives on the ready
+// barrier.
+NMG_D bool signal_ready(int g, bool leader, uint64_t* ready, bool ok) {
   tc::fence_proxy_async();
   tc::fence_before_sync();
-  ok = bar_red_and(1 + g, kRows, ok);
-  if (ok && t == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(ready)) : "memory");
+  ok = bar_red_and(1 + g, 2 * kRows, ok);
+  if (ok && leader) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(tc::smem_u32(ready)) : "memory");
   return ok;
 }
 
@@ -171,21 +170,23 @@ NMG_D void scatter_level(const FusedArgs& a, float* gt, int lv, const float (&p3
 
 // Scatter warps (SCAT): the CTA adds 7 warps (with the issuer warp they form
 // two more warpgroups) that apply each tile's grid gradient to the table
-// while the compute warpgroups move on to their next tile. A compute group
-// stages its layer-0 data gradient in its third hidden tile (dead by then,
-// rewritten only at the next tile's third forward layer) and arrives on
-// sfull; the scatter warps arrive on sempty when they have read it.
-// Registers: the 512-thread block launches at 128 per thread and moves 40
-// of them from the issuer/scatter warpgroups to the compute warpgroups.
-constexpr int kScatRegLaunch = 128, kScatRegCompute = 168, kScatRegScatter = 88;
-static_assert(2 * kRows * kScatRegCompute + 2 * kRows * kScatRegScatter == 4 * kRows * kScatRegLaunch,
+// while the pipelines move on to their next tile. A pipeline stages its
+// layer-0 data gradient in its third hidden tile (dead by then, rewritten
+// only at the next tile's third forward layer) and arrives on sfull; the
+// scatter warps arrive on sempty when they have read it.
+// Registers: the 768-thread block launches at 80 per thread and moves 32 of
+// them from each issuer/scatter thread to the compute threads.
+constexpr int kScatThreadsPerCta = 6 * kRows;
+constexpr int kScatRegLaunch = 80, kScatRegCompute = 96, kScatRegScatter = 48;
+static_assert(4 * kRows * kScatRegCompute + 2 * kRows * kScatRegScatter == kScatThreadsPerCta * kScatRegLaunch,
               "register split must equal the launch allocation");
 
 template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH, int NWG, bool SCAT,
           bool REC>
-__global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
+__global__ void __launch_bounds__(SCAT ? kScatThreadsPerCta : 2 * NWG * kRows + 32, 1)
     k_fused_train(const __grid_constant__ TrainArgs ta) {
-  static_assert(!SCAT || NWG == 2, "scatter warps pair with two compute warpgroups");
+  static_assert(!SCAT || NWG == 2, "scatter warps pair with two pipelines");
+  static_assert(K % 8 == 0, "each half of a row holds K / 2 lobes, a whole number of 16-column groups");
   constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
   constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
   constexpr int NGRID = LEVELS * F;
@@ -193,13 +194,15 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   constexpr uint32_t A_BYTES = kRows * NENC * 2;
   constexpr uint32_t H_BYTES = kRows * kWidth * 2;
   constexpr uint32_t D_BYTES = kRows * DMAX * 2;
-  // per warpgroup, after its operand tiles: each row's GuidedOutput (records
-  // mode REC: computed at the load stage, read at the loss stage) and, by
-  // tile parity, each row's normalised position for the scatter warps
+  // per pipeline, after its operand tiles: each row's GuidedOutput (records
+  // mode REC: computed at the load stage, read at the loss stage), by tile
+  // parity each row's normalised position for the scatter warps, and the
+  // loss's partial sums of both halves of each row
   constexpr uint32_t REC_BYTES = REC ? kRows * 8 * 4 : 0, P3_BYTES = SCAT ? 2 * kRows * 4 * 4 : 0;
-  constexpr uint32_t WG_BYTES = A_BYTES + 3 * H_BYTES + D_BYTES + REC_BYTES + P3_BYTES;
+  constexpr uint32_t XCH_BYTES = 2 * kRows * 2 * 4;
+  constexpr uint32_t WG_BYTES = A_BYTES + 3 * H_BYTES + D_BYTES + REC_BYTES + P3_BYTES + XCH_BYTES;
   constexpr int NL = 4;  // three hidden layers
-  // TMEM: one forward/data-gradient accumulator per warpgroup, then the shared
+  // TMEM: one forward/data-gradient accumulator per pipeline, then the shared
   // weight-gradient accumulators (M = 64) dW0 | dW1 | dW2 | dW3^T.
   constexpr uint32_t DCOLS = NOUTMAX <= 64 ? 64 : 128;
   constexpr uint32_t CW0 = NWG * DCOLS, CW1 = CW0 + NENC, CW2 = CW1 + kWidth, CW3 = CW2 + kWidth;
@@ -210,16 +213,18 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
 
   const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-  const bool issuer = warp == NWG * 4;
-  const bool scatter = SCAT && warp > NWG * 4;
-  const int g = (issuer || scatter) ? 0 : threadIdx.x / kRows;
-  const int t = threadIdx.x % kRows;
+  const bool issuer = warp == NWG * 8;
+  const bool scatter = SCAT && warp > NWG * 8;
+  const int g = (issuer || scatter) ? 0 : warp / 8;  // pipeline
+  const int h = (warp / 4) & 1;                     // half of the row's pair
+  const int t = threadIdx.x % kRows;                // row of the tile
   uint8_t* wsm = smem;
   uint8_t* A0 = smem + w_region + g * WG_BYTES;
   uint8_t* Hs = A0 + A_BYTES;  // three hidden tiles
   uint8_t* Dt = Hs + 3 * H_BYTES;
   float* s_rec = reinterpret_cast<float*>(Dt + D_BYTES);             // [kRows][8]
   float* s_p3 = reinterpret_cast<float*>(Dt + D_BYTES + REC_BYTES);  // [2][kRows][4]
+  float2* s_xch = reinterpret_cast<float2*>(Dt + D_BYTES + REC_BYTES + P3_BYTES);  // [2 halves][kRows]
   // [0] weights, then ready[], done[], sfull[], sempty[]
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NWG * WG_BYTES);
   uint64_t* ready = bars + 1;
@@ -336,7 +341,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
     // Tiles in the order the compute groups finish them (k-th tile of group
     // 0, then of group 1, ...); items (level, row) with rows fastest, so a
     // warp reads consecutive rows of the staged [feature][row] gradient.
-    const int sidx = int(threadIdx.x) - (NWG * 4 + 1) * 32;
+    const int sidx = int(threadIdx.x) - (NWG * 8 + 1) * 32;
     float* gt = ta.grad + ta.n_mlp;
     for (int k = 0; ok; ++k) {
       bool any = false;
@@ -369,13 +374,19 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
     }
     tc::reg_alloc<kScatRegLaunch>();
   } else {
-    // ------------------------------------------------- compute warpgroup g
+    // ---------------------------------------- pipeline g, half h of every row
     if constexpr (SCAT) tc::reg_alloc<kScatRegCompute>();
+    constexpr int KH = K / 2;          // lobes of each half: raw columns [2K h, 2K h + 2K)
+    constexpr int HC = kWidth / 16;    // 8-column chunks of a hidden row per half
+    constexpr int GCH = NGRID / 8;     // 8-column grid chunks; half h owns those with ch % 2 == h
+    constexpr int LPC = 8 / F;         // levels per grid chunk
     uint32_t dph = 0;
+    const bool leader = h == 0 && t == 0;
+    const bool sel_on = a.selection != 0;
     const uint32_t tD = tbase + g * DCOLS;
     const uint32_t lane_addr = (uint32_t((warp & 3) * 32) << 16);
     for (int tile = blockIdx.x * NWG + g; tile < ntiles; tile += gridDim.x * NWG) {
-      const int kt = (tile - (blockIdx.x * NWG + g)) / (gridDim.x * NWG);  // this group's tile number
+      const int kt = (tile - (blockIdx.x * NWG + g)) / (gridDim.x * NWG);  // this pipeline's tile number
       const long q = long(tile) * kRows + t;
       const bool valid = q < n;
       float x[10];
@@ -384,82 +395,121 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
       if (valid) {
         if constexpr (REC) {
           // records mode: the vertex's network input and GuidedOutput from the radiance records
+          // (both halves compute the input; half 0 keeps the GuidedOutput for the loss stage)
           const uint32_t v = ta.vid[ta.id_base + q];
           const uint32_t dd = v / ta.pixels;
           float out[7];
           vertex_record(ta.rr.depth[dd], ta.rr.product, a.enc, v - dd * ta.pixels, x, out);
+          if (h == 0) {
 #pragma unroll
-          for (int j = 0; j < 7; ++j) s_rec[t * 8 + j] = out[j];
+            for (int j = 0; j < 7; ++j) s_rec[t * 8 + j] = out[j];
+          }
         } else {
           load_row(ta.x, q, a.enc.n_input, x);
         }
       }
       if constexpr (SCAT) {  // the scatter warps read this tile's positions from here (buffer kt & 1)
-        float* p3 = s_p3 + (kt & 1) * kRows * 4 + t * 4;
-        p3[0] = x[0];
-        p3[1] = x[1];
-        p3[2] = x[2];
+        if (h == 0) {
+          float* p3 = s_p3 + (kt & 1) * kRows * 4 + t * 4;
+          p3[0] = x[0];
+          p3[1] = x[1];
+          p3[2] = x[2];
+        }
       }
-      encode_row<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, false>(a, x, A0, t);
-      ok = signal_ready(g, t, &ready[g], ok);
+      encode_row_half<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, true>(a, x, A0, t, h);
+      ok = signal_ready(g, leader, &ready[g], ok);
       if (!ok) break;
 
       // ---------------------------------------------------------- forward
-      float r[NOUTMAX];
-#pragma unroll
-      for (int i = 0; i < NOUTMAX; ++i) r[i] = 0.f;
+      float rh[2 * K];  // this half's lobes' raw outputs
+      float sel_logit = 0.f;
       for (int l = 0; l < NL; ++l) {
         const bool fin = tc::mbar_wait(&done[g], dph);
         dph ^= 1u;
         tc::fence_after_sync();
         if (l < NL - 1) {
-          float v[kWidth];
-          tc::tmem_load<kWidth / 16>(tD + lane_addr, v);
+          float v[kWidth / 2];
+          tc::tmem_load<kWidth / 32>(tD + lane_addr + uint32_t(h * (kWidth / 2)), v);
           uint8_t* H = Hs + l * H_BYTES;
           bool free_h = true;
           if (SCAT && l == 2 && kt > 0)  // the scatter warps still read the previous tile's gradient here
             free_h = tc::mbar_wait(&sempty[g], uint32_t(kt - 1) & 1u);
 #pragma unroll
-          for (int c = 0; c < kWidth / 8; ++c) store_chunk_relu(H, t, c, kWidth / 8, v + 8 * c, fp16);
-          ok = signal_ready(g, t, &ready[g], fin && free_h && ok);
+          for (int c = 0; c < HC; ++c) store_chunk_relu(H, t, h * HC + c, kWidth / 8, v + 8 * c, fp16);
+          ok = signal_ready(g, leader, &ready[g], fin && free_h && ok);
           if (!ok) break;
         } else {
-          tc::tmem_load_n<NOUTMAX / 16>(tD + lane_addr, r, (nout + 15) / 16);
+          tc::tmem_load<K / 8>(tD + lane_addr + uint32_t(h * 2 * K), rh);
+          if (sel_on) {
+            float v[16];
+            tc::tmem_load<1>(tD + lane_addr + uint32_t(4 * K), v);
+            sel_logit = v[0];
+          }
           ok = fin && ok;
         }
       }
       if (!ok) {
-        ok = bar_red_and(1 + g, kRows, false);
+        ok = bar_red_and(1 + g, 2 * kRows, false);
         break;
       }
 
       // ------------------------------------------------- loss and adjoint
+      // each half takes its KH lobes; the lobe-weight total and the weighted
+      // vMF sum of the other half come through shared memory
       {
-        float gr[NOUTMAX];
+        float rr[8];
 #pragma unroll
-        for (int i = 0; i < NOUTMAX; ++i) gr[i] = 0.f;
+        for (int j = 0; j < 8; ++j) rr[j] = 0.f;
         if (valid) {
-          float rr[8];
           if constexpr (REC) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j) rr[j] = j < 7 ? s_rec[t * 8 + j] : 0.f;
+            for (int j = 0; j < 7; ++j) rr[j] = s_rec[t * 8 + j];
           } else {
 #pragma unroll
             for (int j = 0; j < 8; ++j) rr[j] = j < ta.rstride ? ta.rec[q * ta.rstride + j] : 0.f;
           }
-          loss_acc += double(tile_loss<K, NOUTMAX>(ta, r, rr, scale, gr));
         }
+        HalfLoss<KH> hl;
+        half_loss_lobes<KH, true>(hl, rh, rr, a.mix);
+        const float2 mine = valid ? make_float2(hl.lt, hl.nt) : make_float2(0.f, 0.f);
+        s_xch[h * kRows + t] = mine;
+        ok = bar_red_and(1 + g, 2 * kRows, ok);  // a bar.red, like every other barrier of the pipeline
+        if (!ok) break;
+        const float2 other = s_xch[(1 - h) * kRows + t];
+        float gh[4 * KH];
+        float gsel = 0.f;
+        const float l = sel_on ? half_loss_grad<KH, true, true>(hl, mine.x + other.x, mine.y + other.y, sel_logit, rr,
+                                                                scale, a.mix, gh, &gsel)
+                               : half_loss_grad<KH, true, false>(hl, mine.x + other.x, mine.y + other.y, 0.f, rr,
+                                                                 scale, a.mix, gh, &gsel);
+        if (valid && h == 0) loss_acc += double(l);
+        // delta columns: half 0 its lobes' [0, 2K); half 1 its lobes' [2K, 4K),
+        // the selection logit's gradient (column 4K) and zero padding to nout
+        if (h == 0) {
 #pragma unroll
-        for (int c = 0; c < NOUTMAX / 8; ++c) {
-          if (c * 8 < nout) {
+          for (int c = 0; c < K / 4; ++c) {
             float fv[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) fv[i] = gr[8 * c + i] * S;
+            for (int i = 0; i < 8; ++i) fv[i] = valid ? gh[8 * c + i] * S : 0.f;
             store_chunk(Dt, t, c, KC3, fv, fp16);
+          }
+        } else {
+#pragma unroll
+          for (int c = K / 4; c < NOUTMAX / 8; ++c) {
+            if (c * 8 < nout) {
+              float fv[8];
+#pragma unroll
+              for (int i = 0; i < 8; ++i) {
+                const int col = 8 * c + i;
+                const float gv = col < 4 * K ? gh[col < 4 * K ? col - 2 * K : 0] : (col == 4 * K ? gsel : 0.f);
+                fv[i] = valid ? gv * S : 0.f;
+              }
+              store_chunk(Dt, t, c, KC3, fv, fp16);
+            }
           }
         }
       }
-      ok = signal_ready(g, t, &ready[g], ok);
+      ok = signal_ready(g, leader, &ready[g], ok);
       if (!ok) break;
 
       // ---------------------------------------------------------- backward
@@ -467,56 +517,69 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
         const bool fin = tc::mbar_wait(&done[g], dph);
         dph ^= 1u;
         tc::fence_after_sync();
-        float v[kWidth];
-        tc::tmem_load<kWidth / 16>(tD + lane_addr, v);
+        float v[kWidth / 2];
+        tc::tmem_load<kWidth / 32>(tD + lane_addr + uint32_t(h * (kWidth / 2)), v);
         const uint8_t* H = Hs + (l - 1) * H_BYTES;
 #pragma unroll
-        for (int c = 0; c < kWidth / 8; ++c) {
+        for (int c = 0; c < HC; ++c) {
           float hv[8], fv[8];
-          load_chunk(H, t, c, kWidth / 8, hv, fp16);
+          load_chunk(H, t, h * HC + c, kWidth / 8, hv, fp16);
 #pragma unroll
           for (int i = 0; i < 8; ++i) fv[i] = hv[i] > 0.f ? v[8 * c + i] : 0.f;
-          store_chunk(Dt, t, c, kWidth / 8, fv, fp16);
+          store_chunk(Dt, t, h * HC + c, kWidth / 8, fv, fp16);
         }
-        ok = signal_ready(g, t, &ready[g], fin && ok);
+        ok = signal_ready(g, leader, &ready[g], fin && ok);
         if (!ok) break;
       }
       if (!ok) break;
-      // layer 0: dL/d(grid features) -> table gradient
+      // layer 0: dL/d(grid features) -> table gradient (each half its own grid chunks)
       {
         const bool fin = tc::mbar_wait(&done[g], dph);
         dph ^= 1u;
         tc::fence_after_sync();
         float dg[NGRID];
         tc::tmem_load<NGRID / 16>(tD + lane_addr, dg);
-        ok = bar_red_and(1 + g, kRows, fin && ok);
+        ok = bar_red_and(1 + g, 2 * kRows, fin && ok);
         if (!ok) break;
         if constexpr (SCAT) {
           // hand the gradient to the scatter warps through the third hidden tile
           float* dgs = reinterpret_cast<float*>(Hs + 2 * H_BYTES);
           static_assert(NGRID * kRows * 4 <= H_BYTES, "grid gradient staging fits a hidden tile");
 #pragma unroll
-          for (int j = 0; j < NGRID; ++j) dgs[j * kRows + t] = dg[j] * inv_S;
-          ok = bar_red_and(1 + g, kRows, ok);
+          for (int ch = 0; ch < GCH; ++ch)
+            if ((ch & 1) == h) {
+#pragma unroll
+              for (int i = 0; i < 8; ++i) dgs[(8 * ch + i) * kRows + t] = dg[8 * ch + i] * inv_S;
+            }
+          ok = bar_red_and(1 + g, 2 * kRows, ok);
           if (!ok) break;
-          if (t == 0) tc::mbar_arrive(&sfull[g]);
+          if (leader) tc::mbar_arrive(&sfull[g]);
           continue;
         }
         // Stage the row's grid gradient in the (now idle) delta tile, column t,
-        // so the level loop below can index it: [feature][row] floats.
+        // so the level loop below can index it: [feature][row] floats; each
+        // half stages and scatters the levels of its own chunks.
         float* dgs = reinterpret_cast<float*>(Dt);
         static_assert(NGRID * kRows * 4 <= D_BYTES, "grid gradient staging fits the delta tile");
 #pragma unroll
-        for (int j = 0; j < NGRID; ++j) dgs[j * kRows + t] = dg[j] * inv_S;
+        for (int ch = 0; ch < GCH; ++ch)
+          if ((ch & 1) == h) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) dgs[(8 * ch + i) * kRows + t] = dg[8 * ch + i] * inv_S;
+          }
         if (valid) {
           const float p3[3] = {x[0], x[1], x[2]};
           float* gt = ta.grad + ta.n_mlp;
 #pragma unroll 1
-          for (int lv = 0; lv < LEVELS; ++lv) {
-            float df[F];
+          for (int ch = h; ch < GCH; ch += 2) {
+#pragma unroll 1
+            for (int j = 0; j < LPC; ++j) {
+              const int lv = ch * LPC + j;
+              float df[F];
 #pragma unroll
-            for (int k = 0; k < F; ++k) df[k] = dgs[(F * lv + k) * kRows + t];
-            scatter_level<F, SMOOTH>(a, gt, lv, p3, df);
+              for (int k = 0; k < F; ++k) df[k] = dgs[(F * lv + k) * kRows + t];
+              scatter_level<F, SMOOTH>(a, gt, lv, p3, df);
+            }
           }
         }
       }
@@ -531,13 +594,14 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   if (ok && cta_tiles > 0 && !issuer && !scatter) {
     const int row = (warp & 3) * 16 + lane;  // valid for lane < 16
     const uint32_t qaddr = uint32_t((warp & 3) * 32) << 16;
-    // one accumulator per layer m, warpgroup m % NWG flushing it; the layer's
-    // TMEM column and width are compile-time constants (no runtime-indexed
-    // local arrays: a build that held them on the stack read every layer from
-    // column 0)
+    // one accumulator per layer m, compute warpgroup m % (2 NWG) flushing it;
+    // the layer's TMEM column and width are compile-time constants (no
+    // runtime-indexed local arrays: a build that held them on the stack read
+    // every layer from column 0)
+    const int cwg = warp / 4;
 #pragma unroll
     for (int m = 0; m < 4; ++m) {
-      if (m % NWG != g) continue;
+      if (m % (2 * NWG) != cwg) continue;
       const uint32_t col_m = m == 0 ? CW0 : (m == 1 ? CW1 : (m == 2 ? CW2 : CW3));
       const int width_m = m == 0 ? NENC : kWidth;
       const int ncols = m == 3 ? nout : width_m;
@@ -561,7 +625,7 @@ __global__ void __launch_bounds__(SCAT ? 4 * kRows : NWG * kRows + 32, 1)
   if (!ok && threadIdx.x == 0) atomicExch(a.err, 3);
   // loss partial sum of this CTA
   {
-    __shared__ double red[SCAT ? 16 : NWG * 4 + 1];
+    __shared__ double red[SCAT ? kScatThreadsPerCta / 32 : NWG * 8 + 1];
     double v = (issuer || scatter) ? 0.0 : loss_acc;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -602,11 +666,12 @@ static nmg_status launch_train(const TrainArgs& a, int grid, cudaStream_t st) {
   }
   const size_t smem = size_t((a.f.w_bytes + 1023u) & ~1023u) +
                       NWG * (size_t(kRows) * NENC * 2 + 3 * size_t(kRows) * kWidth * 2 + size_t(kRows) * DW * 2 +
-                             (REC ? size_t(kRows) * 8 * 4 : 0) + (SCAT ? 2 * size_t(kRows) * 4 * 4 : 0)) +
+                             (REC ? size_t(kRows) * 8 * 4 : 0) + (SCAT ? 2 * size_t(kRows) * 4 * 4 : 0) +
+                             2 * size_t(kRows) * 2 * 4) +
                       256;
   nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
   if (s != NMG_OK) return s;
-  kern<<<grid, SCAT ? 4 * kRows : NWG * kRows + 32, smem, st>>>(a);
+  kern<<<grid, SCAT ? kScatThreadsPerCta : 2 * NWG * kRows + 32, smem, st>>>(a);
   return check_launch("k_fused_train");
 }
 

@@ -620,4 +620,100 @@ NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float s
   return loss;
 }
 
+// The same loss (train.cu:69-172) with the lobes split over two threads
+// that each hold KH of them. Part one (half_loss_lobes) computes the
+// thread's lobes' activations and vMF values at the record's direction and
+// the partial sums of the lobe weights and of the weighted vMF values; the
+// caller adds the partner's partial sums; part two (half_loss_grad) forms q =
+// sum(lam vmf) / sum(lam) and the thread's lobe gradients (and, SEL, the
+// selection logit's). Lobe arithmetic and precision as mix_kl_loss_grad.
+template <int KH> struct HalfLoss {
+  float lam[KH], kap[KH], dkap[KH], vmf[KH], cc[KH], dta[KH], dpa[KH], sgt[KH], sgp[KH];
+  float lt, nt;
+};
+
+template <int KH, bool FAST, int PRECISE = !FAST, class RAW>
+NMG_D void half_loss_lobes(HalfLoss<KH>& s, const RAW& raw, const float* rec, const MixOpts& o) {
+  float swt, cwt, swp, cwp;
+  xsincos<FAST && !PRECISE>(rec[0], &swt, &cwt);
+  xsincos_2pi<FAST && !PRECISE>(rec[1], &swp, &cwp);
+  const f3 wi{swt * cwp, swt * swp, cwt};
+  s.lt = 0.f;
+  s.nt = 0.f;
+#pragma unroll
+  for (int i = 0; i < KH; ++i) {
+    const float4 r = lobe4(raw, i);
+    s.lam[i] = xexp<FAST>(act_exp_clamp(r.x));
+    if (o.kappa_softplus) {
+      s.kap[i] = softplus<FAST>(r.y);
+      s.dkap[i] = logistic<FAST>(r.y);
+    } else {
+      s.kap[i] = xexp<FAST>(act_exp_clamp(r.y));
+      s.dkap[i] = s.kap[i];  // train.h:410: derivative ignores the clamp
+    }
+    s.sgt[i] = logistic<FAST>(r.z);
+    s.sgp[i] = logistic<FAST>(r.w);
+    float sth, cth, sph, cph;
+    lobe_angles<FAST, PRECISE, false>(s.sgt[i], s.sgp[i], &sth, &cth, &sph, &cph);
+    s.cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
+    s.dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
+    s.dpa[i] = (wi.y * cph - wi.x * sph) * sth;
+    const float k = s.kap[i];
+    s.vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, s.cc[i] - 1.f)) * vmf_norm<FAST>(k);
+    s.lt += s.lam[i];
+    s.nt += s.lam[i] * s.vmf[i];
+  }
+}
+
+// total / nt_total: both threads' sums; sel_logit: raw output 4K (SEL).
+// Writes grad[4 KH] (and *gsel when SEL); returns the per-sample loss.
+template <int KH, bool FAST, bool SEL>
+NMG_D float half_loss_grad(const HalfLoss<KH>& s, float total, float nt_total, float sel_logit, const float* rec,
+                           float scale, const MixOpts& o, float* grad, float* gsel) {
+  const float inv_total = 1.f / total;
+  const float q = nt_total * inv_total;
+  const float Li = (rec[2] + (rec[3] + rec[4])) / 3.f;
+  float prefix, loss, sel = 1.f;
+  if (SEL) {
+    sel = logistic<FAST>(sel_logit);
+    const float wp = sel * (q + NMG_EPS) + (1.f - sel) * rec[6];
+    loss = -Li / wp * logf(wp);
+    prefix = -Li / wp / wp * scale;
+    *gsel = 0.01f * prefix * (q - rec[6]) * (sel * (1.f - sel));
+  } else {
+    const float wp = rec[5] + NMG_EPS, guide = q + NMG_EPS;
+    prefix = -Li / wp / guide * scale;
+    loss = -Li / wp * logf(guide);
+  }
+#pragma unroll
+  for (int i = 0; i < KH; ++i) {
+    const float k = s.kap[i];
+    const float wv = (s.lam[i] * inv_total) * s.vmf[i];
+    float ik;
+    if (o.kappa_poly && k < 1.f) {
+      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+    } else if (!o.kappa_poly && k < 1e-2f) {
+      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+    } else {
+      const float e = xexp<FAST>(-2.f * k);
+      ik = 1.f / k - (1.f + e) / (1.f - e);
+    }
+    float g0 = prefix * ((s.vmf[i] - q) * inv_total * sel) * s.lam[i];
+    float g1 = prefix * (wv * (s.cc[i] + ik) * sel) * s.dkap[i];
+    float g2 = prefix * (wv * k * s.dta[i] * sel) * NMG_PI * (s.sgt[i] * (1.f - s.sgt[i]));
+    float g3 = prefix * (wv * k * s.dpa[i] * sel) * NMG_TWO_PI * (s.sgp[i] * (1.f - s.sgp[i]));
+    if (!SEL) {  // train.cu:109-123 (the selection variant has no such pass)
+      g0 = isfinite(g0) ? fminf(g0, 150.f) : 0.f;
+      g1 = isfinite(g1) ? fminf(g1, 150.f) : 0.f;
+      g2 = isfinite(g2) ? fminf(g2, 150.f) : 0.f;
+      g3 = isfinite(g3) ? fminf(g3, 150.f) : 0.f;
+    }
+    grad[4 * i + 0] = g0;
+    grad[4 * i + 1] = g1;
+    grad[4 * i + 2] = g2;
+    grad[4 * i + 3] = g3;
+  }
+  return loss;
+}
+
 }  // namespace nmg
