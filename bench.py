@@ -325,7 +325,7 @@ def run_ours(args):
     step_qps, step_tps = ws * N_QUERIES * steps / t_step, ws * N_TRAIN * steps / t_step
     qps = ws * N_QUERIES * steps / ours["t_query"]
     tps = ws * N_TRAIN * steps / ours["t_train"]
-    p_steps = max(1, min(args.steps, 3)) if path != nmg.PATH_FP32 else steps
+    p_steps = steps  # the plain path runs the same steps as the measured one
     plain_qps = N_QUERIES * p_steps / plain["t_query"]
     plain_tps = N_TRAIN * p_steps / plain["t_train"]
     plain_step_qps = N_QUERIES * p_steps / (plain["t_query"] + plain["t_train"])
