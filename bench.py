@@ -43,11 +43,11 @@ FLOP_PER_QUERY = 2 * (80 * 64 + 64 * 64 + 64 * 64 + 64 * 48)  # 32,768 executed 
 BYTES_PER_QUERY = 12 + 12 + 12 + 4 + 16 + 12 + 4 + 4 + 4      # pos, wo, n, rough, u4 in; dir, pdf, lobe, sel out
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_fused_query_ws launch over the same
 # 2,073,600-query wavefront (ncu capture summarised in profiles/k_fused_query_ws_hashgrid_2073600.md)
-TRAFFIC_QUERY_BYTES = 141_328_128 + 35_287_040
+TRAFFIC_QUERY_BYTES = 141_316_608 + 35_742_464
 # l1tex__m_xbar2l1tex_read_bytes.sum of the same capture: the hash-grid corner gathers reaching L2
 # (the 24 MB table stays in L2), in 32-byte sectors; about one sector request per cycle per SM is
 # the ceiling a gather-only kernel of the same 128 corners per query reaches
-L2_TO_L1_BYTES = 4.697e9
+L2_TO_L1_BYTES = 4.686e9
 
 
 # The hash-grid network (NMG_PRESET_HASHGRID) as the oracle describes it; the CPU legs build it from this

@@ -315,9 +315,8 @@ class GuidingField:
     def operand_params(self, which=1):
         """The parameter values the fused kernels multiply, as FP32 (None on the plain FP32 path):
         the grid table in the path's 16-bit format; the MLP of the training image (which = 0) all in
-        that format; the MLP of the inference image (which = 1, the query and pdf passes) on the BF16
-        path as bf16(W0) + bf16(W0 - bf16(W0)) for the first layer and FP16 for the later layers, on
-        the FP16 path all FP16."""
+        that format; the MLP of the inference image (which = 1, the query and pdf passes) in FP16 on
+        both 16-bit paths."""
         import torch
         if self.cfg.path == PATH_FP32:
             return None
@@ -327,10 +326,7 @@ class GuidingField:
             return p.to(torch.float16).float()
         out = p.to(torch.bfloat16).float()
         if which == 1:
-            n0 = int(self.info.n_encoded_padded) * int(self.cfg.width)
-            hi = p[:n0].to(torch.bfloat16).float()
-            out[:n0] = hi + (p[:n0] - hi).to(torch.bfloat16).float()
-            out[n0:n_mlp] = p[n0:n_mlp].to(torch.float16).float()
+            out[:n_mlp] = p[:n_mlp].to(torch.float16).float()
         return out
 
     def get_gradients(self):

@@ -294,21 +294,20 @@ nmg_status fused_reserve(nmg_ctx* c) {
   s.w_bytes = (off + 15u) & ~15u;
   // Operand formats. The FP16 path: every layer FP16. The BF16 path: the
   // training image all BF16; the inference image (the query and pdf passes)
-  // keeps BF16 for the first layer, whose input is the BF16 encoding, and
-  // adds W0's BF16 low parts, then FP16 for the hidden and output layers.
-  // Against the FP64 network on the FP32 weights this brings the query's pdf
-  // error from 1.8e-3 to about 5e-4 at the maximum over 65,536 queries
-  // (hidden activations of this bias-free ReLU network are O(1); FP16's 11
-  // significant bits instead of BF16's 8 carry most of the gain, the low
-  // parts of W0 the rest), for 10 KB more shared memory and one more pass of
-  // the first layer's MMAs.
+  // runs the whole MLP on FP16 operands over the BF16 grid table: the encoder
+  // packs the input tile in FP16 (the interpolated BF16 table values and the
+  // direction encodings are then carried more precisely than in BF16).
+  // Against the FP64 network on the FP32 weights, all-BF16 operands left a pdf
+  // error of 1.8e-3 at the maximum over 65,536 queries; the hidden
+  // activations of this bias-free ReLU network are O(1), within FP16's range,
+  // and its 11 significant bits instead of BF16's 8 carry the precision.
   const bool all16 = c->cfg.path == NMG_PATH_FP16;
   const uint32_t all_layers = (1u << L.n_layers) - 1u;
   s.pack.fp16_layers[0] = all16 ? all_layers : 0u;
   s.pack.w0_lo_off[0] = 0;
-  s.pack.fp16_layers[1] = all16 ? all_layers : all_layers & ~1u;
-  s.pack.w0_lo_off[1] = all16 ? 0u : (off + 127u) & ~127u;
-  s.w_bytes_inf = all16 ? s.w_bytes : (s.pack.w0_lo_off[1] + uint32_t(L.in[0]) * uint32_t(L.out[0]) * 2u + 15u) & ~15u;
+  s.pack.fp16_layers[1] = all_layers;
+  s.pack.w0_lo_off[1] = 0;
+  s.w_bytes_inf = s.w_bytes;
   const size_t head = 256;
   const size_t bytes = head + size_t(s.w_bytes) + size_t(s.w_bytes_inf);
   void* mem = nullptr;
