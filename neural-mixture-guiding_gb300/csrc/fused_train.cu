@@ -204,7 +204,10 @@ __global__ void __launch_bounds__(SCAT ? kScatThreadsPerCta : 2 * NWG * kRows + 
   constexpr int NL = 4;  // three hidden layers
   // TMEM: one forward/data-gradient accumulator per pipeline, then the shared
   // weight-gradient accumulators (M = 64) dW0 | dW1 | dW2 | dW3^T.
-  constexpr uint32_t DCOLS = NOUTMAX <= 64 ? 64 : 128;
+  // (the accumulator holds a hidden layer's 64 columns or the output layer's
+  // NOUTMAX: 80 for 16 lobes, so that two pipelines and the weight gradients
+  // fit the 512 columns)
+  constexpr uint32_t DCOLS = NOUTMAX <= kWidth ? kWidth : (NOUTMAX + 15) / 16 * 16;
   constexpr uint32_t CW0 = NWG * DCOLS, CW1 = CW0 + NENC, CW2 = CW1 + kWidth, CW3 = CW2 + kWidth;
   static_assert(CW3 + NOUTMAX <= kTrainCols, "TMEM holds 512 columns");
   static_assert(NGRID <= 64 && NGRID % 16 == 0, "grid features are read in 16-column groups");
@@ -706,7 +709,7 @@ nmg_status fused_train_step_src(nmg_ctx* c, const float* x, const float* rec, co
   a.partials = c->ws.partials;
   const int sms = sm_count();
   const int tiles = (n_max + kRows - 1) / kRows;
-  const int per_cta = s->preset == 2 ? 1 : 2;  // warpgroups (tiles in flight) per CTA
+  const int per_cta = 2;  // pipelines (tiles in flight) per CTA
   int grid = (tiles + per_cta - 1) / per_cta < sms ? (tiles + per_cta - 1) / per_cta : sms;
   if (grid < 1) grid = 1;
   if (grid > c->ws.n_partials / 2) grid = c->ws.n_partials / 2;
@@ -722,8 +725,8 @@ nmg_status fused_train_step_src(nmg_ctx* c, const float* x, const float* rec, co
                : launch_train<2, 16, 1, 4, 4, 8, 48, false, 2, true, false>(a, grid, st);
       break;
     case 2:
-      r = recs ? launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false, true>(a, grid, st)
-               : launch_train<2, 16, 1, 4, 4, 16, 80, false, 1, false, false>(a, grid, st);
+      r = recs ? launch_train<2, 16, 1, 4, 4, 16, 80, false, 2, true, true>(a, grid, st)
+               : launch_train<2, 16, 1, 4, 4, 16, 80, false, 2, true, false>(a, grid, st);
       break;
     case 3:
       r = recs ? launch_train<4, 8, 0, 2, 4, 8, 48, true, 2, true, true>(a, grid, st)

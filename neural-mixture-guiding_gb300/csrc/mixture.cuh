@@ -622,13 +622,18 @@ NMG_D float mix_kl_loss_grad_selection(const RAW& raw, const float* rec, float s
 
 // The same loss (train.cu:69-172) with the lobes split over two threads
 // that each hold KH of them. Part one (half_loss_lobes) computes the
-// thread's lobes' activations and vMF values at the record's direction and
-// the partial sums of the lobe weights and of the weighted vMF values; the
-// caller adds the partner's partial sums; part two (half_loss_grad) forms q =
-// sum(lam vmf) / sum(lam) and the thread's lobe gradients (and, SEL, the
-// selection logit's). Lobe arithmetic and precision as mix_kl_loss_grad.
+// thread's lobes' activations and vMF values at the record's direction, the
+// partial sums of the lobe weights and of the weighted vMF values, and
+// folds each lobe's derivative factors into three numbers, so that only five
+// values per lobe stay live while the caller adds the partner's partial
+// sums; part two (half_loss_grad) forms q = sum(lam vmf) / sum(lam) and the
+// thread's lobe gradients (and, SEL, the selection logit's). Lobe arithmetic
+// and precision as mix_kl_loss_grad.
 template <int KH> struct HalfLoss {
-  float lam[KH], kap[KH], dkap[KH], vmf[KH], cc[KH], dta[KH], dpa[KH], sgt[KH], sgp[KH];
+  float lam[KH], vmf[KH];
+  float dk[KH];  // (cos + I(kappa)) dkappa/dx: the kappa gradient's factor
+  float dt[KH];  // kappa dmu/dtheta . wi * pi sigma'(x_theta): the theta gradient's factor
+  float dp[KH];  // kappa dmu/dphi . wi * 2 pi sigma'(x_phi): the phi gradient's factor
   float lt, nt;
 };
 
@@ -643,25 +648,37 @@ NMG_D void half_loss_lobes(HalfLoss<KH>& s, const RAW& raw, const float* rec, co
 #pragma unroll
   for (int i = 0; i < KH; ++i) {
     const float4 r = lobe4(raw, i);
-    s.lam[i] = xexp<FAST>(act_exp_clamp(r.x));
+    const float lam = xexp<FAST>(act_exp_clamp(r.x));
+    float kap, dkap;
     if (o.kappa_softplus) {
-      s.kap[i] = softplus<FAST>(r.y);
-      s.dkap[i] = logistic<FAST>(r.y);
+      kap = softplus<FAST>(r.y);
+      dkap = logistic<FAST>(r.y);
     } else {
-      s.kap[i] = xexp<FAST>(act_exp_clamp(r.y));
-      s.dkap[i] = s.kap[i];  // train.h:410: derivative ignores the clamp
+      kap = xexp<FAST>(act_exp_clamp(r.y));
+      dkap = kap;  // train.h:410: derivative ignores the clamp
     }
-    s.sgt[i] = logistic<FAST>(r.z);
-    s.sgp[i] = logistic<FAST>(r.w);
+    const float sgt = logistic<FAST>(r.z), sgp = logistic<FAST>(r.w);
     float sth, cth, sph, cph;
-    lobe_angles<FAST, PRECISE, false>(s.sgt[i], s.sgp[i], &sth, &cth, &sph, &cph);
-    s.cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
-    s.dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
-    s.dpa[i] = (wi.y * cph - wi.x * sph) * sth;
-    const float k = s.kap[i];
-    s.vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, s.cc[i] - 1.f)) * vmf_norm<FAST>(k);
-    s.lt += s.lam[i];
-    s.nt += s.lam[i] * s.vmf[i];
+    lobe_angles<FAST, PRECISE, false>(sgt, sgp, &sth, &cth, &sph, &cph);
+    const float cc = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
+    const float k = kap;
+    const float vmf = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, cc - 1.f)) * vmf_norm<FAST>(k);
+    float ik;
+    if (o.kappa_poly && k < 1.f) {
+      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+    } else if (!o.kappa_poly && k < 1e-2f) {
+      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+    } else {
+      const float e = xexp<FAST>(-2.f * k);
+      ik = 1.f / k - (1.f + e) / (1.f - e);
+    }
+    s.lam[i] = lam;
+    s.vmf[i] = vmf;
+    s.dk[i] = (cc + ik) * dkap;
+    s.dt[i] = k * (cth * (wi.x * cph + wi.y * sph) - wi.z * sth) * (NMG_PI * (sgt * (1.f - sgt)));
+    s.dp[i] = k * ((wi.y * cph - wi.x * sph) * sth) * (NMG_TWO_PI * (sgp * (1.f - sgp)));
+    s.lt += lam;
+    s.nt += lam * vmf;
   }
 }
 
@@ -687,21 +704,11 @@ NMG_D float half_loss_grad(const HalfLoss<KH>& s, float total, float nt_total, f
   }
 #pragma unroll
   for (int i = 0; i < KH; ++i) {
-    const float k = s.kap[i];
-    const float wv = (s.lam[i] * inv_total) * s.vmf[i];
-    float ik;
-    if (o.kappa_poly && k < 1.f) {
-      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
-    } else if (!o.kappa_poly && k < 1e-2f) {
-      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
-    } else {
-      const float e = xexp<FAST>(-2.f * k);
-      ik = 1.f / k - (1.f + e) / (1.f - e);
-    }
+    const float pw = prefix * ((s.lam[i] * inv_total) * s.vmf[i] * sel);  // prefix * wv * sel
     float g0 = prefix * ((s.vmf[i] - q) * inv_total * sel) * s.lam[i];
-    float g1 = prefix * (wv * (s.cc[i] + ik) * sel) * s.dkap[i];
-    float g2 = prefix * (wv * k * s.dta[i] * sel) * NMG_PI * (s.sgt[i] * (1.f - s.sgt[i]));
-    float g3 = prefix * (wv * k * s.dpa[i] * sel) * NMG_TWO_PI * (s.sgp[i] * (1.f - s.sgp[i]));
+    float g1 = pw * s.dk[i];
+    float g2 = pw * s.dt[i];
+    float g3 = pw * s.dp[i];
     if (!SEL) {  // train.cu:109-123 (the selection variant has no such pass)
       g0 = isfinite(g0) ? fminf(g0, 150.f) : 0.f;
       g1 = isfinite(g1) ? fminf(g1, 150.f) : 0.f;
