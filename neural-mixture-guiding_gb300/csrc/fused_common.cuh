@@ -414,23 +414,25 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
       }
     }
     sel = sel < 0 ? 0 : sel;
-    float ks = 0.f;
-    f3 ms{0.f, 0.f, 1.f};
+    // the selected lobe's four raw outputs, picked from each group as it is read (the reads are
+    // warp-collective, the lobe is each thread's own), then that one lobe derived
+    float rs[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) rs[k] = 0.f;
 #pragma unroll
     for (int g = 0; g < G; ++g) {
       float v[16];
       tc::tmem_load<1>(lane_addr + 16 * g, v);
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
-        float lam, kap, nrm;
-        f3 mu;
-        lobe(v, j, lam, kap, mu, nrm);
-        if (4 * g + j == sel) {
-          ks = kap;
-          ms = mu;
-        }
+        const bool pick = 4 * g + j == sel;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) rs[k] = pick ? v[4 * j + k] : rs[k];
       }
     }
+    float lam, ks, nrm;
+    f3 ms;
+    lobe(rs, 0, lam, ks, ms, nrm);
     d = vmf_sample_dir<true>(ks, ms, u.z, u.w);
   }
   // pass 3: pdf at d (distribution.h:113-119)
