@@ -339,14 +339,15 @@ nmg_status nmg_network_vjp(nmg_ctx* ctx, const float* x, const float* draw, int 
 /*
  * Tiling of the fused query kernel: warpgroups (128-query tiles in flight)
  * per CTA, one CTA per SM; 5 and 6 are valid when the padded output width is
- * <= 64. 8-12 select configurations of the warp-specialised kernel: encoder
+ * <= 64. 7: two tiles in flight, each on two warpgroups, two threads per
+ * query splitting the lobes (queries that return raw outputs fall back to
+ * 4). 8-12 select configurations of the warp-specialised kernel: encoder
  * warpgroups feed MLP + mixture warpgroups through a shared-memory ring
  * (8: 4 + 2 warpgroups, 4 slots; 9: 5 + 1, 5 slots; 10: 6 + 2, 6 slots;
  * 11: 4 + 2, 8 slots; 12: 4 + 2, 4 slots holding the hidden activations too).
  * 0 selects the default: 12 for the 8-lobe hash-grid network, 8 for the
- * reference network, 4 for 16-lobe networks. A tiling whose shared memory
- * exceeds the device's limit for this network's weight image (11 on the BF16
- * path, whose query weights carry a second first-layer image) makes the
+ * reference network, 7 for 16-lobe networks. A tiling whose shared memory
+ * exceeds the device's limit for this network's weight image makes the
  * query calls return NMG_ERR_UNSUPPORTED; the autotuner skips it.
  * nmg_get_query_tiling
  * reports the tiling in use (0 on the FP32 path). No counterpart in the

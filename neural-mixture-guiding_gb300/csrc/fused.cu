@@ -161,6 +161,261 @@ __global__ void __launch_bounds__(NWG * kRows, 1) k_fused_query(const __grid_con
   }
 }
 
+// Tiling 7: two pipelines per CTA, each two warpgroups on one 128-query tile
+// (the layout of the training kernel): warps w and w + 4 read the same TMEM
+// lane quadrant, so every query has two threads, which split the encoding's
+// grid levels, each hidden epilogue's columns and the mixture's lobes. With
+// K / 2 lobes per thread the lobes stay in registers from activation to pdf
+// (one pass, where one thread holding all 16 re-derives them from TMEM);
+// the lobe-weight total, the selection scan (continued by the second half
+// where the first half's lobes ran out, the reference's sequential
+// subtraction), the sampled lobe and the pdf's partial sums cross between
+// the two through shared memory. Queries without raw outputs only.
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
+__global__ void __launch_bounds__(4 * kRows, 1) k_fused_query_pair(const __grid_constant__ FusedArgs a) {
+  constexpr int NP = 2, KH = K / 2;
+  static_assert(K % 8 == 0, "each half holds K / 2 lobes, whole 16-column TMEM groups");
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
+  constexpr uint32_t TILE_BYTES = kRows * (NENC > kWidth ? NENC : kWidth) * 2;
+  constexpr uint32_t COLS = NOUTMAX <= kWidth ? kWidth : (NOUTMAX + 15) / 16 * 16;  // TMEM columns per pipeline
+  constexpr uint32_t TCOLS = COLS * NP <= 128 ? 128 : 256;
+  static_assert(COLS * NP <= 256, "two pipelines' accumulators within 256 columns");
+  constexpr int XCH = 2 * kRows * 8;  // exchange floats per pipeline: [half][row][8]
+  extern __shared__ __align__(1024) uint8_t smem[];
+
+  const uint32_t w_region = (a.w_bytes + 1023u) & ~1023u;
+  const int warp = threadIdx.x / 32;
+  const int p = warp / 8, h = (warp / 4) & 1, t = threadIdx.x % kRows;
+  const bool leader = h == 0 && t == 0;
+  uint8_t* wsm = smem;
+  uint8_t* A = smem + w_region + p * TILE_BYTES;
+  float* xch = reinterpret_cast<float*>(smem + w_region + NP * TILE_BYTES) + p * XCH;
+  float* mine = xch + (h * kRows + t) * 8;
+  const float* other = xch + ((1 - h) * kRows + t) * 8;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem + w_region + NP * TILE_BYTES + NP * XCH * 4);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bars + 1 + NP);
+
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&bars[0], 1);
+    for (int i = 0; i < NP; ++i) tc::mbar_init(&bars[1 + i], 1);
+    tc::fence_mbar_init();
+  }
+  if (threadIdx.x < 32) tc::tmem_alloc(tslot, TCOLS);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  if (threadIdx.x == 0) {
+    tc::mbar_arrive_expect_tx(&bars[0], a.w_bytes);
+    for (uint32_t off = 0; off < a.w_bytes; off += 16384u) {
+      const uint32_t nb = a.w_bytes - off < 16384u ? a.w_bytes - off : 16384u;
+      tc::bulk_g2s(wsm + off, a.wimg + off, nb, &bars[0]);
+    }
+  }
+  bool ok = tc::mbar_wait(&bars[0], 0);
+  ok = __syncthreads_and(ok) != 0;
+  if (!ok && threadIdx.x == 0) atomicExch(a.err, 1);
+
+  const uint32_t tmem = *tslot + uint32_t(p) * COLS;
+  const uint32_t lane_addr = tmem + (uint32_t((warp & 3) * 32) << 16);
+  uint64_t* bar = &bars[1 + p];
+  uint32_t phase = 0;
+  const int n = fused_count(a.d_count, a.n_max);
+  const int ntiles = (n + kRows - 1) / kRows;
+  const int nl = a.n_layers;
+  const uint32_t a_addr = tc::smem_u32(A);
+  const bool cosine = a.mix.cosine != 0;
+  const float nb = prod_norm<true>(kCosineKappa);
+
+  // Every named barrier is a bar.red.and over the pipeline's 256 threads, and
+  // every early exit follows one, so the two warpgroups always leave together.
+  for (int tile = blockIdx.x * NP + p; tile < ntiles; tile += gridDim.x * NP) {
+    const long q = long(tile) * kRows + t;
+    const bool valid = q < n;
+    float x[10];
+#pragma unroll
+    for (int d = 0; d < 10; ++d) x[d] = 0.f;
+    f3 wo3{0.f, 0.f, 1.f}, n3{0.f, 0.f, 1.f};
+    if (valid) {
+      wo3 = load3(a.wo, q);
+      n3 = load3(a.nrm, q);
+      featurize<true>(a.enc, load3(a.pos, q), wo3, n3, a.rough[q], x);
+    }
+    encode_row_half<F, LEVELS, MODE, SHDEG, BINS, SMOOTH, true>(a, x, A, t, h);
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    ok = bar_red_and(1 + p, 2 * kRows, ok);
+    if (!ok) break;
+    // ---- MLP; this half's columns of each hidden layer, its lobes' raw outputs
+    float rh[2 * K];
+    float sel_logit = 0.f;
+    bool last_ok = true;
+    for (int l = 0; l < nl; ++l) {
+      const bool last = l == nl - 1;
+      const int kin = l == 0 ? NENC : kWidth;
+      const int nout = last ? a.n_out_pad : kWidth;
+      if (leader) {
+        tc::fence_after_sync();
+        issue_layer(a, l, tmem, a_addr, tc::smem_u32(wsm), kin, nout);
+        tc::mma_commit(bar);
+      }
+      const bool done = tc::mbar_wait(bar, phase);
+      phase ^= 1u;
+      tc::fence_after_sync();
+      if (!last) {
+        float v[kWidth / 2];
+        tc::tmem_load<kWidth / 32>(lane_addr + uint32_t(h * (kWidth / 2)), v);
+#pragma unroll
+        for (int c = 0; c < kWidth / 16; ++c)
+          store_chunk_relu(A, t, h * (kWidth / 16) + c, kWidth / 8, v + 8 * c, layer_fp16(a, l + 1));
+        tc::fence_proxy_async();
+        tc::fence_before_sync();
+        ok = bar_red_and(1 + p, 2 * kRows, done);
+        if (!ok) break;
+      } else {
+        tc::tmem_load<K / 8>(lane_addr + uint32_t(h * 2 * K), rh);
+        if (a.selection) {
+          float v[16];
+          tc::tmem_load<1>(lane_addr + uint32_t(4 * K), v);
+          sel_logit = v[0];
+        }
+        last_ok = done;
+      }
+    }
+    if (!ok) break;
+    ok = bar_red_and(1 + p, 2 * kRows, last_ok);
+    if (!ok) break;
+    // ---- mixture: lobes [KH h, KH h + KH) (distribution.h:85-98, 184-195)
+    f3 mb{0.f, 0.f, 1.f};
+    if (cosine && valid) mb = unit3<true>(face_fwd(n3, wo3));
+    float lam[KH], kap[KH], nrm[KH];
+    f3 mu[KH];
+    float part = 0.f;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) {
+      lobe_activate<true>(rh[4 * i], rh[4 * i + 1], rh[4 * i + 2], rh[4 * i + 3], a.mix.kappa_softplus, lam[i],
+                          kap[i], mu[i]);
+      nrm[i] = vmf_norm<true>(kap[i]);
+      if (cosine) lobe_cosine<true>(mb, nb, lam[i], kap[i], mu[i], nrm[i]);
+      part += lam[i];
+    }
+    mine[0] = part;
+    ok = bar_red_and(1 + p, 2 * kRows, ok);
+    if (!ok) break;
+    float total = h == 0 ? part + other[0] : other[0] + part;
+    if (cosine) total = fmaxf(total, NMG_EPS);  // distribution.h:191
+    const float inv = 1.f / total;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) lam[i] *= inv;  // the lobe weights from here on
+    f3 d{0.f, 0.f, 1.f};
+    int sel = 0;
+    if (a.wi) {
+      if (valid) d = load3(a.wi, q);
+    } else {
+      // selection (distribution.h:132-140): half 0 scans its lobes with u and
+      // hands the rest of u to half 1, which continues where lobe KH - 1 left off
+      const float4 u = valid ? reinterpret_cast<const float4*>(a.u4)[q] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float ks = kap[0];
+      f3 ms = mu[0];
+      if (h == 0) {
+        float uu = u.y;
+        int s0 = -1;
+#pragma unroll
+        for (int i = 0; i < KH; ++i) {
+          if (s0 < 0) {
+            if (uu < lam[i])
+              s0 = i;
+            else
+              uu -= lam[i];
+          }
+        }
+#pragma unroll
+        for (int i = 1; i < KH; ++i)
+          if (i == s0) {
+            ks = kap[i];
+            ms = mu[i];
+          }
+        mine[1] = __int_as_float(s0);
+        mine[2] = uu;
+        mine[3] = ks;  // lobe s0's, or lobe 0's when none of these was selected (the fallback)
+        mine[4] = ms.x;
+        mine[5] = ms.y;
+        mine[6] = ms.z;
+      }
+      ok = bar_red_and(1 + p, 2 * kRows, ok);
+      if (!ok) break;
+      if (h == 1) {
+        const int s0 = __float_as_int(other[1]);
+        sel = s0;
+        ks = other[3];
+        ms = f3{other[4], other[5], other[6]};
+        if (s0 < 0) {
+          float uu = other[2];
+          int s1 = -1;
+#pragma unroll
+          for (int i = 0; i < KH; ++i) {
+            if (s1 < 0) {
+              if (uu < lam[i])
+                s1 = i;
+              else
+                uu -= lam[i];
+            }
+          }
+          sel = 0;  // no lobe selected: lobe 0, whose parameters half 0 handed over
+          if (s1 >= 0) {
+            sel = KH + s1;
+#pragma unroll
+            for (int i = 0; i < KH; ++i)
+              if (i == s1) {
+                ks = kap[i];
+                ms = mu[i];
+              }
+          }
+        }
+        mine[1] = __int_as_float(sel);
+        mine[3] = ks;
+        mine[4] = ms.x;
+        mine[5] = ms.y;
+        mine[6] = ms.z;
+      }
+      ok = bar_red_and(1 + p, 2 * kRows, ok);
+      if (!ok) break;
+      if (h == 0) {
+        sel = __float_as_int(other[1]);
+        ks = other[3];
+        ms = f3{other[4], other[5], other[6]};
+      }
+      d = vmf_sample_dir<true>(ks, ms, u.z, u.w);  // the same inputs in both halves
+    }
+    // pdf at d (distribution.h:113-119), this half's lobes
+    float pd = 0.f;
+#pragma unroll
+    for (int i = 0; i < KH; ++i) {
+      const float c = dot3(d, mu[i]);
+      const float v = kap[i] < NMG_EPS ? NMG_INV_4PI : __expf(kap[i] * fminf(0.f, c - 1.f)) * nrm[i];
+      pd += lam[i] * v;
+    }
+    mine[7] = pd;
+    ok = bar_red_and(1 + p, 2 * kRows, ok);
+    if (!ok) break;
+    if (h == 0 && valid) {
+      a.pdf[q] = pd + other[7];
+      if (!a.wi) {
+        store3(a.dir, q, d);
+        if (a.lobe) a.lobe[q] = sel;
+      }
+      if (a.sel && a.selection) a.sel[q] = logistic<true>(sel_logit);
+    }
+  }
+  if (!ok && t == 0) atomicExch(a.err, 2);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc::fence_after_sync();
+    tc::tmem_dealloc(*tslot, TCOLS);
+  }
+}
+
 // ------------------------------------------------------------ weight image
 // Element (n, k) of layer l goes to byte layer_off[l] + cm_offset(n, k/8,
 // in_l/8) + 2 (k % 8): each layer becomes a K-major operand of N = out_l rows,
@@ -244,22 +499,52 @@ static nmg_status launch_query(const FusedArgs& a, int nwg, cudaStream_t st) {
   return launch_query_nwg<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH, 4>(a, st);
 }
 
+template <int F, int LEVELS, int MODE, int SHDEG, int BINS, int K, int NOUTMAX, bool SMOOTH>
+static nmg_status launch_query_pair(const FusedArgs& a, cudaStream_t st) {
+  constexpr int NDIR = MODE == 0 ? SHDEG * SHDEG + 3 * BINS : 2 * SHDEG * SHDEG + BINS;
+  constexpr int NENC = (LEVELS * F + NDIR + 15) / 16 * 16;
+  auto kern = k_fused_query_pair<F, LEVELS, MODE, SHDEG, BINS, K, NOUTMAX, SMOOTH>;
+  const size_t smem = size_t((a.w_bytes + 1023u) & ~1023u) +
+                      2 * (size_t(kRows) * (NENC > kWidth ? NENC : kWidth) * 2 + 2 * size_t(kRows) * 8 * 4) + 128;
+  nmg_status s = ensure_smem(reinterpret_cast<const void*>(kern), smem);
+  if (s != NMG_OK) return s;
+  const int sms = sm_count();
+  const int tiles = (a.n_max + kRows - 1) / kRows;
+  int grid = (tiles + 1) / 2;
+  if (grid > sms) grid = sms;
+  if (grid < 1) grid = 1;
+  kern<<<grid, 4 * kRows, smem, st>>>(a);
+  return check_launch("k_fused_query_pair");
+}
+
 // Default query tiling: the warp-specialised kernel (4 encoder + 2 consumer
 // warpgroups) for the 8-lobe networks, measured 1.3x faster than one
 // pipeline per warpgroup on a 2,073,600-query wavefront; for the hash-grid
 // network its variant with the hidden activations kept in the ring slot
 // (tiling 12: 32 KB more L1 for the table gathers) measured 630 us against
 // 646 us. The 16-lobe network's consumer epilogue does not fit 128
-// registers, so it keeps the one-pipeline-per-warpgroup kernel.
+// registers: it takes tiling 7, two threads per query with 8 lobes each in
+// registers, 1.096 ms on a 2,073,600-query wavefront against 1.266 ms for one
+// pipeline per warpgroup re-deriving the lobes from TMEM and 1.344 ms for the
+// warp-specialised kernel (for 8 lobes tiling 7 measured 0.952 ms against
+// 0.643 ms for tiling 12).
 int fused_default_tiling(const nmg_ctx* c) {
   const FusedState* s = reinterpret_cast<const FusedState*>(c->ws.fused);
-  if (!s || s->preset == 2) return 4;
+  if (!s) return 4;
+  if (s->preset == 2) return kTilingPair;
   return s->preset == 1 ? kTilingWarpSpecialised + 4 : kTilingWarpSpecialised;
 }
 
 static nmg_status dispatch_query(nmg_ctx* c, const FusedArgs& a, cudaStream_t st) {
   const int nwg = c->query_wg > 0 ? c->query_wg : fused_default_tiling(c);
   if (nwg >= kTilingWarpSpecialised) return launch_query_ws(fstate(c)->preset, nwg, a, st);
+  if (nwg == kTilingPair && !a.raw && !a.raw_mode) {
+    switch (fstate(c)->preset) {
+      case 1: return launch_query_pair<2, 16, 1, 4, 4, 8, 48, false>(a, st);
+      case 2: return launch_query_pair<2, 16, 1, 4, 4, 16, 80, false>(a, st);
+      case 3: return launch_query_pair<4, 8, 0, 2, 4, 8, 48, true>(a, st);
+    }
+  }
   switch (fstate(c)->preset) {
     case 1: return launch_query<2, 16, 1, 4, 4, 8, 48, false>(a, nwg, st);
     case 2: return launch_query<2, 16, 1, 4, 4, 16, 80, false>(a, nwg, st);
@@ -447,8 +732,8 @@ nmg_status fused_check_errors(nmg_ctx* c) {
 // Candidate CTA shapes of the fused query kernel: 4, 5 or 6 warpgroups
 // (128-query tiles) per CTA, one CTA per SM. More warpgroups hide more
 // gather and MMA latency but cap registers (128, 102, 85 per thread).
-static const int kTileCandidates[] = {4, 5, 6, 8, 9, 10, 11, 12};
-static const int kTileCandidatesK16[] = {4, 8};  // 128 TMEM columns per warpgroup
+static const int kTileCandidates[] = {4, 5, 6, 7, 8, 9, 10, 11, 12};
+static const int kTileCandidatesK16[] = {4, 7, 8};  // 128 TMEM columns per warpgroup
 
 static std::string tune_cache_path() {
   const char* p = getenv("NMG_TUNE_CACHE");

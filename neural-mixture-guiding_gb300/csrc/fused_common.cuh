@@ -501,6 +501,7 @@ FusedArgs fused_make_args(nmg_ctx* c, bool infer_weights);
 // 9 = 5 + 1, 5 slots; 10 = 6 + 2, 6 slots; 11 = 4 + 2, 8 slots;
 // 12 = 4 + 2, 4 slots, hidden activations kept in the slot.
 constexpr int kTilingWarpSpecialised = 8;
+constexpr int kTilingPair = 7;  // two pipelines of two warpgroups, two threads per query (queries without raw outputs)
 constexpr int kTilingLast = 12;
 nmg_status launch_query_ws(int preset, int tiling, const FusedArgs& a, cudaStream_t st);
 

@@ -465,11 +465,11 @@ nmg_status nmg_network_vjp(nmg_ctx* c, const float* x, const float* draw, int n,
 
 nmg_status nmg_set_query_tiling(nmg_ctx* c, int warpgroups_per_cta) {
   NMG_REQUIRE(c != nullptr, "ctx is NULL");
-  NMG_REQUIRE(warpgroups_per_cta == 0 || (warpgroups_per_cta >= 4 && warpgroups_per_cta <= 6) ||
-                  (warpgroups_per_cta >= 8 && warpgroups_per_cta <= 12),
-              "warpgroups_per_cta=%d (0 = default, 4..6, or 8..12 = warp-specialised)", warpgroups_per_cta);
-  NMG_REQUIRE(warpgroups_per_cta == 4 || warpgroups_per_cta == 8 || warpgroups_per_cta == 0 ||
-                  c->lay.n_out_pad <= 64,
+  NMG_REQUIRE(warpgroups_per_cta == 0 || (warpgroups_per_cta >= 4 && warpgroups_per_cta <= 12),
+              "warpgroups_per_cta=%d (0 = default, 4..6, 7 = two threads per query, 8..12 = warp-specialised)",
+              warpgroups_per_cta);
+  NMG_REQUIRE(warpgroups_per_cta == 4 || warpgroups_per_cta == 7 || warpgroups_per_cta == 8 ||
+                  warpgroups_per_cta == 0 || c->lay.n_out_pad <= 64,
               "tiling %d needs <= 64 outputs", warpgroups_per_cta);
   c->query_wg = warpgroups_per_cta;
   return NMG_OK;

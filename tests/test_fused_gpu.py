@@ -354,3 +354,33 @@ def test_fused_tilings_agree_and_autotune(nmg, synth, tmp_path, monkeypatch):
     assert f.autotune(pos, wo, n, r, u4, use_cache=True) == chosen  # served from the cache
     f.check_errors()
     f.close()
+
+
+@pytest.mark.parametrize("preset,K", [(1, 8), (1, 16), (0, 8)], ids=["hash-K8", "hash-K16", "reference-K8"])
+def test_pair_tiling_matches_one_thread_per_query(nmg, synth, preset, K):
+    """Tiling 7 (two threads per query, the lobes split between them, the selection scan continued by
+    the second thread) samples the same lobes and directions and evaluates the same pdfs as tiling 4 (one
+    thread per query) on the same inputs, up to the order of the lobe sums and instruction-level
+    contraction: sampling, and the pdf at given directions."""
+    f = nmg.GuidingField(nmg.config(preset, path=1, n_lobes=K), max_queries=50000)
+    perturb(f, 7)
+    q = synth.wavefront(50000, seed=23)
+    pos, wo, n, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
+    f.set_query_tiling(4)
+    ref = f.query(pos, wo, n, r, u4)
+    pref = f.pdf(pos, wo, n, r, ref["dir"])
+    f.set_query_tiling(7)
+    out = f.query(pos, wo, n, r, u4)
+    pout = f.pdf(pos, wo, n, r, ref["dir"])
+    same = out["lobe"] == ref["lobe"]
+    assert float(same.float().mean()) >= 0.999
+    assert float((out["dir"] - ref["dir"])[same].abs().max()) <= 5e-2
+    assert float(((out["dir"] - ref["dir"])[same]).pow(2).mean().sqrt()) <= 1e-3
+    rel = (out["pdf"] - ref["pdf"])[same].abs() / ref["pdf"][same]
+    assert float(rel.pow(2).mean().sqrt()) <= 1e-3
+    relp = (pout - pref).abs() / pref
+    assert float(relp.pow(2).mean().sqrt()) <= 1e-3
+    if "selection" in ref:
+        assert float((out["selection"] - ref["selection"]).abs().max()) <= 1e-3
+    f.check_errors()
+    f.close()
