@@ -174,7 +174,7 @@ def run_ours(args):
         a separate field, so the timed steps are the field's first steps after its warm-up (gradient norm
         reported per step), not steps of a network that hundreds of load steps at the configured learning
         rate drove into the exp clamp."""
-        cfg = nmg.config(nmg.PRESET_HASHGRID, path=path_id)
+        cfg = nmg.config(nmg.PRESET_HASHGRID, path=path_id, n_lobes=args.lobes)
         f = nmg.GuidingField(cfg, max_queries=N_QUERIES, max_batch=N_TRAIN)
         src = synth.TorchTrainSource(synth.TrainField(seed=replica_seed(rank)), seed=replica_seed(rank) + 3)
         out = {"dir": torch.empty((N_QUERIES, 3), device="cuda"), "pdf": torch.empty(N_QUERIES, device="cuda"),
@@ -757,10 +757,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-frame", action="store_true", help="skip the 7-bounce CUDA-graph frame measurement")
+    ap.add_argument("--lobes", type=int, default=8, choices=[8, 16],
+                    help="mixture lobes of the network (the measured line is quoted on 8; 16 for --steps-only profiling)")
     ap.add_argument("--steps-only", action="store_true",
                     help="time only the guiding steps (no CPU leg, plain path, frame, mixture or other rows); "
                          "the small command the ncu captures in profiles/ run")
     args = ap.parse_args()
+    if args.lobes != 8 and not args.steps_only:
+        ap.error("--lobes 16 only with --steps-only: the measured line is the 8-lobe configuration")
     if args.impl == "reference":
         run_reference(args)
     else:
