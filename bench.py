@@ -176,6 +176,8 @@ def run_ours(args):
         rate drove into the exp clamp."""
         cfg = nmg.config(nmg.PRESET_HASHGRID, path=path_id, n_lobes=args.lobes)
         f = nmg.GuidingField(cfg, max_queries=N_QUERIES, max_batch=N_TRAIN)
+        if args.tiling and path_id != nmg.PATH_FP32:
+            f.set_query_tiling(args.tiling)
         src = synth.TorchTrainSource(synth.TrainField(seed=replica_seed(rank)), seed=replica_seed(rank) + 3)
         out = {"dir": torch.empty((N_QUERIES, 3), device="cuda"), "pdf": torch.empty(N_QUERIES, device="cuda"),
                "lobe": torch.empty(N_QUERIES, device="cuda", dtype=torch.int32),
@@ -256,6 +258,12 @@ def run_ours(args):
                "loss": st_np[steps - 1].tolist(), "health": health, "field": f, "out": out}
         return res
 
+    if args.mixture_only:
+        # the mixture-only kernels' row alone, for profiling
+        if rank == 0:
+            print(json.dumps({"mixture_only": True, "mixture_kernels": mixture_kernels(nmg, synth, torch, flush,
+                                                                                     peaks()[0])}), flush=True)
+        return
     if args.steps_only:
         # the guiding step alone, for profiling: `warmup` + `steps` steps of a fresh field (no clock
         # sampler, no other measurements); the line carries only the step times
@@ -762,7 +770,13 @@ def main():
     ap.add_argument("--steps-only", action="store_true",
                     help="time only the guiding steps (no CPU leg, plain path, frame, mixture or other rows); "
                          "the small command the ncu captures in profiles/ run")
+    ap.add_argument("--tiling", type=int, default=0,
+                    help="fused query tiling (0 = the default), with --steps-only, for profiling one kernel")
+    ap.add_argument("--mixture-only", action="store_true",
+                    help="time only the mixture-only kernels (no network), for profiling them")
     args = ap.parse_args()
+    if args.tiling and not args.steps_only:
+        ap.error("--tiling only with --steps-only: the measured line uses the default tiling")
     if args.lobes != 8 and not args.steps_only:
         ap.error("--lobes 16 only with --steps-only: the measured line is the 8-lobe configuration")
     if args.impl == "reference":
