@@ -301,7 +301,9 @@ def run_ours(args):
     e2e_step()  # first call allocates the device staging
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
-    e2e_steps = max(1, min(args.steps, 5))
+    # back-to-back steps from an idle GPU, as a renderer issues them frame after frame: the first
+    # step's input copy is exposed, the later ones run under the previous step's kernels
+    e2e_steps = max(20, args.steps)
     e0.record()
     for _ in range(e2e_steps):
         e2e_step()
@@ -376,8 +378,9 @@ def run_ours(args):
         "train_health": ours["health"],
         "e2e": {"value": ws * N_QUERIES * e2e_steps / t_e2e, "unit": "queries/s",
                 "what": "query pass + training step per step, host buffers in and out",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                "api": "nmg_query_host + nmg_train_step_host (pinned host memory)", "final_loss": e2e_loss},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                "api": "nmg_query_host + nmg_train_step_host (pinned host memory; inputs copied in, results "
+                       "written by the kernels through the host mapping)", "final_loss": e2e_loss},
         "gpu_launches": None,
         "roofline": {"kernel": "k_fused_query_ws" if path != nmg.PATH_FP32 else "plain query kernels",
                      "bound": "tensor", "achieved": tflops, "peak": bf16, "unit": "TFLOP/s",

@@ -302,22 +302,27 @@ nmg_status nmg_train_step(nmg_ctx* ctx, const float* x, const float* records, co
 
 /*
  * nmg_query and nmg_train_step on HOST buffers (pinned memory gives the
- * overlap; pageable memory works but copies synchronously). nmg_query_host
- * splits the wavefront into up to 4 chunks of at least 2^18 queries and
- * pipelines them over three streams: inputs of chunk i+1 go to the device
- * while chunk i is computed on `stream` and the outputs of chunk i-1 come
- * back. Every input and output array (all of in, u4, out->dir, out->pdf and,
- * when non-NULL, out->lobe and out->selection) is host memory; out->raw must
- * be NULL. nmg_train_step_host copies x and records to the device and runs
- * the step; stats (may be NULL) is HOST memory receiving the two FP64
- * statistics. Their kernels run on `stream` after the work already queued
- * there and `stream` waits for their last copy; the input copies start as
- * soon as the previous call's kernels have read the device staging, so they
- * overlap other work still running on `stream` (the host input arrays must
- * therefore be filled before the call, and all host buffers stay valid
- * until `stream` reaches the call's end). The first call allocates device
- * staging of the reserved capacity (not capturable); later calls allocate
- * nothing.
+ * overlap; pageable memory works but copies synchronously). Every input and
+ * output array (all of in, u4, out->dir, out->pdf and, when non-NULL,
+ * out->lobe and out->selection) is host memory; out->raw must be NULL.
+ * nmg_query_host copies the inputs on a stream of its own into one of two
+ * alternating device staging buffers; the copies wait only for the kernels
+ * of the call before the previous one, so they overlap other work still
+ * running on `stream` (the previous query and training step, for instance).
+ * When `stream` is idle at the call, the wavefront is split into up to 4
+ * chunks of at least 2^18 queries, so that chunk i+1's inputs are copied
+ * while chunk i is computed (nmg_set_host_chunks fixes the count). When every
+ * output given is pinned (page-locked) host memory, the query kernel writes
+ * the results there itself through the host mapping; otherwise they are
+ * staged on the device and copied back on a third stream.
+ * nmg_train_step_host copies x and records to the device and runs the step;
+ * stats (may be NULL) is HOST memory receiving the two FP64 statistics
+ * (written by the kernel when pinned). The kernels of both calls run on
+ * `stream` after the work already queued there, and `stream` waits for their
+ * last copy: the host input arrays must be filled before the call, and all
+ * host buffers stay valid until `stream` reaches the call's end. The first
+ * call allocates device staging of the reserved capacity (not capturable);
+ * later calls allocate nothing.
  * Replaces: the host side of the reference's inference/training calls, which
  * copy nothing themselves (integrator.cpp:627-701 operate on device queues);
  * no reference counterpart as an entry point.
@@ -326,6 +331,16 @@ nmg_status nmg_query_host(nmg_ctx* ctx, const nmg_shading* in, const float* u4, 
                           nmg_stream stream);
 nmg_status nmg_train_step_host(nmg_ctx* ctx, const float* x, const float* records, int n, double* stats,
                                nmg_stream stream);
+
+/*
+ * Number of chunks nmg_query_host splits a wavefront into: 0 (the default)
+ * chooses 1 when `stream` has work queued at the call and up to 4 when it is
+ * idle; 1..8 fixes it (chunks stay at least 2^18 queries, so a small
+ * wavefront may get fewer). nmg_get_host_chunks returns the fixed count, or
+ * 4 when automatic. No reference counterpart (tuning).
+ */
+nmg_status nmg_set_host_chunks(nmg_ctx* ctx, int chunks);
+int nmg_get_host_chunks(const nmg_ctx* ctx);
 
 /*
  * Vector-Jacobian product of the network at the training weights:

@@ -202,6 +202,7 @@ def _bind_field(L):
         "nmg_frame_run_eager": [P, C.POINTER(Bounce), C.c_int, P],
         "nmg_network_vjp": [P, P, P, C.c_int, P, P, P],
         "nmg_set_query_tiling": [P, C.c_int],
+        "nmg_set_host_chunks": [P, C.c_int],
         "nmg_autotune_query": [P, C.POINTER(Shading), P, C.c_int, C.POINTER(QueryOut), C.c_int, C.POINTER(C.c_int), P],
         "nmg_check_errors": [P],
         "nmg_selftest_wait_timeout": [P, P],
@@ -223,6 +224,8 @@ def _bind_field(L):
     L.nmg_get_step.restype = C.c_int
     L.nmg_get_query_tiling.argtypes = [P]
     L.nmg_get_query_tiling.restype = C.c_int
+    L.nmg_get_host_chunks.argtypes = [P]
+    L.nmg_get_host_chunks.restype = C.c_int
     L.nmg_frame_nodes.argtypes = [P]
     L.nmg_frame_nodes.restype = C.c_int
     L.nmg_frame_destroy.argtypes = [P]
@@ -459,6 +462,14 @@ class GuidingField:
     @property
     def query_tiling(self):
         return self.L.nmg_get_query_tiling(self.h)
+
+    def set_host_chunks(self, chunks):
+        """Most chunks query_host splits a wavefront into (0 = automatic)."""
+        check(self.L.nmg_set_host_chunks(self.h, int(chunks)))
+
+    @property
+    def host_chunks(self):
+        return self.L.nmg_get_host_chunks(self.h)
 
     def autotune(self, pos, wo, normal, rough, u4, use_cache=False, stream=None):
         """Picks the fastest fused-query tiling on these inputs; returns it."""

@@ -62,6 +62,7 @@ struct nmg_ctx {
   uint16_t* w16 = nullptr;     // training weights
   uint16_t* w16_inf = nullptr; // inference weights
   int query_wg = 0;            // warpgroups per CTA of the fused query kernel (0: default)
+  int host_chunks = 0;         // chunks of nmg_query_host (0: automatic)
   nmg::Workspace ws;
   void* host_io = nullptr;     // streams and staging of the host-buffer entry points (host_io.cu)
 };

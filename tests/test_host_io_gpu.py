@@ -91,3 +91,49 @@ def test_host_steps_interleaved_match_device_steps(nmg, synth):
     a.check_errors()
     for f in (a, b):
         f.close()
+
+
+def test_query_host_slots_chunks_and_output_kinds(nmg, synth):
+    """Queued query_host calls on different inputs (the two input staging slots alternate, the third
+    call reuses the first slot while nothing has synchronised), at 1, 2, 3 and 8 chunks and automatic
+    (4 chunks for the first call on the idle stream, 1 for the two queued behind it), with outputs
+    in pinned memory (written by the kernel through the mapping), in pageable memory (staged and
+    copied back) and mixed (one pageable output stages them all): every result equals the
+    device-buffer query on the same inputs."""
+    import torch
+    n = 800_003
+    keys = ("pos", "wo", "normal", "rough", "u4")
+    f = nmg.GuidingField(nmg.config(1, path=1), max_queries=n)
+    assert f.host_chunks == 4
+    with pytest.raises(nmg.NMGError):
+        f.set_host_chunks(9)
+    with pytest.raises(nmg.NMGError):
+        f.set_host_chunks(-1)
+    qs = [synth.wavefront(n, seed=900 + i) for i in range(3)]
+    hq = [{k: torch.from_numpy(np.ascontiguousarray(q[k])).pin_memory() for k in keys} for q in qs]
+    refs = [f.query(*(h[k].cuda() for k in keys)) for h in hq]
+    torch.cuda.synchronize()
+    refs = [{k: v.cpu() for k, v in r.items() if v is not None} for r in refs]
+
+    def outputs(kind):
+        o = {"dir": torch.empty((n, 3)), "pdf": torch.empty(n), "lobe": torch.empty(n, dtype=torch.int32)}
+        if kind == "pinned":
+            o = {k: v.pin_memory() for k, v in o.items()}
+        elif kind == "mixed":
+            o = {k: (v if k == "pdf" else v.pin_memory()) for k, v in o.items()}
+        return o
+
+    for chunks in (1, 2, 3, 8, 0):
+        f.set_host_chunks(chunks)
+        assert f.host_chunks == (chunks or 4)
+        for kind in ("pinned", "pageable", "mixed"):
+            outs = [outputs(kind) for _ in qs]
+            torch.cuda.synchronize()
+            for h, o in zip(hq, outs):
+                f.query_host(*(h[k] for k in keys), o)
+            torch.cuda.synchronize()
+            for o, r in zip(outs, refs):
+                for k in ("dir", "pdf", "lobe"):
+                    assert torch.equal(o[k], r[k]), (chunks, kind, k)
+    f.check_errors()
+    f.close()
