@@ -613,13 +613,19 @@ __global__ void __launch_bounds__(SCAT ? kScatThreadsPerCta : 2 * NWG * kRows + 
         float v[16];
         tc::tmem_load<1>(tbase + qaddr + col_m + uint32_t(c0), v);
         if (lane < 16) {
+          if (m < 3) {
+            // dW_m[out = row][in = col]: a thread's 16 columns are contiguous, added as 4 float4
+            // (the layer offsets and widths are multiples of 4 floats)
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const int col = c0 + i;
-            if (col >= ncols) continue;
-            const long idx = m < 3 ? off_m + long(row) * width_m + col  // dW_m[out = row][in = col]
-                                   : off_m + long(col) * kWidth + row;  // W3[out = col][in = row]
-            atomicAdd(ta.grad + idx, v[i] * inv_S);
+            for (int i = 0; i < 16; i += 4)
+              if (c0 + i < ncols)
+                atomicAdd(reinterpret_cast<float4*>(ta.grad + off_m + long(row) * width_m + c0 + i),
+                          make_float4(v[i] * inv_S, v[i + 1] * inv_S, v[i + 2] * inv_S, v[i + 3] * inv_S));
+          } else {
+            // W3[out = col][in = row]: the 16 threads' rows are contiguous for each column
+#pragma unroll
+            for (int i = 0; i < 16; ++i)
+              if (c0 + i < ncols) atomicAdd(ta.grad + off_m + long(c0 + i) * kWidth + row, v[i] * inv_S);
           }
         }
       }
@@ -705,7 +711,11 @@ nmg_status fused_train_step_src(nmg_ctx* c, const float* x, const float* rec, co
   a.loss_scale = c->cfg.loss_scale;
   a.grad = c->grad;
   a.n_mlp = c->lay.n_mlp;
-  for (int l = 0; l < c->lay.n_layers; ++l) a.layer_elem_off[l] = c->lay.off[l];
+  for (int l = 0; l < c->lay.n_layers; ++l) {
+    // the weight-gradient flush adds float4 rows of the hidden layers
+    NMG_REQUIRE(c->lay.off[l] % 4 == 0, "layer %d offset %ld not a multiple of 4", l, long(c->lay.off[l]));
+    a.layer_elem_off[l] = c->lay.off[l];
+  }
   a.partials = c->ws.partials;
   const int sms = sm_count();
   const int tiles = (n_max + kRows - 1) / kRows;

@@ -12,6 +12,8 @@
 // __fdividef) for the fused reduced-precision path; FAST = false uses CUDA's
 // accurate expf/sincosf/log1pf for the FP32 path.
 #pragma once
+#include <string.h>
+
 #include "common.cuh"
 
 namespace nmg {
@@ -73,8 +75,9 @@ NMG_HD void sincospi_poly(float t, float* s, float* c) {
   *c = hi ? -ca : ca;
 }
 
-// sin(pi k/32) and cos(pi k/32) for k = 0..64, each rounded once to FP32
-// from an 80-bit long-double evaluation (the multiples of 1/2 are exact).
+// sin(pi k/32) and cos(pi k/32) for k = 0..127 (one period of t = k/32),
+// each rounded once to FP32 from an 80-bit long-double evaluation (the
+// multiples of 1/2 are exact).
 #define NMG_SINCOSPI32_TABLE { \
   {0.000000000e+00f, 1.000000000e+00f}, /* k = 0 */ \
   {9.801714122e-02f, 9.951847196e-01f}, /* k = 1 */ \
@@ -141,22 +144,100 @@ NMG_HD void sincospi_poly(float t, float* s, float* c) {
   {-1.950903237e-01f, 9.807852507e-01f}, /* k = 62 */ \
   {-9.801714122e-02f, 9.951847196e-01f}, /* k = 63 */ \
   {0.000000000e+00f, 1.000000000e+00f}, /* k = 64 */ \
+  {9.801714122e-02f, 9.951847196e-01f}, /* k = 65 */ \
+  {1.950903237e-01f, 9.807852507e-01f}, /* k = 66 */ \
+  {2.902846634e-01f, 9.569403529e-01f}, /* k = 67 */ \
+  {3.826834261e-01f, 9.238795042e-01f}, /* k = 68 */ \
+  {4.713967443e-01f, 8.819212914e-01f}, /* k = 69 */ \
+  {5.555702448e-01f, 8.314695954e-01f}, /* k = 70 */ \
+  {6.343932748e-01f, 7.730104327e-01f}, /* k = 71 */ \
+  {7.071067691e-01f, 7.071067691e-01f}, /* k = 72 */ \
+  {7.730104327e-01f, 6.343932748e-01f}, /* k = 73 */ \
+  {8.314695954e-01f, 5.555702448e-01f}, /* k = 74 */ \
+  {8.819212914e-01f, 4.713967443e-01f}, /* k = 75 */ \
+  {9.238795042e-01f, 3.826834261e-01f}, /* k = 76 */ \
+  {9.569403529e-01f, 2.902846634e-01f}, /* k = 77 */ \
+  {9.807852507e-01f, 1.950903237e-01f}, /* k = 78 */ \
+  {9.951847196e-01f, 9.801714122e-02f}, /* k = 79 */ \
+  {1.000000000e+00f, 0.000000000e+00f}, /* k = 80 */ \
+  {9.951847196e-01f, -9.801714122e-02f}, /* k = 81 */ \
+  {9.807852507e-01f, -1.950903237e-01f}, /* k = 82 */ \
+  {9.569403529e-01f, -2.902846634e-01f}, /* k = 83 */ \
+  {9.238795042e-01f, -3.826834261e-01f}, /* k = 84 */ \
+  {8.819212914e-01f, -4.713967443e-01f}, /* k = 85 */ \
+  {8.314695954e-01f, -5.555702448e-01f}, /* k = 86 */ \
+  {7.730104327e-01f, -6.343932748e-01f}, /* k = 87 */ \
+  {7.071067691e-01f, -7.071067691e-01f}, /* k = 88 */ \
+  {6.343932748e-01f, -7.730104327e-01f}, /* k = 89 */ \
+  {5.555702448e-01f, -8.314695954e-01f}, /* k = 90 */ \
+  {4.713967443e-01f, -8.819212914e-01f}, /* k = 91 */ \
+  {3.826834261e-01f, -9.238795042e-01f}, /* k = 92 */ \
+  {2.902846634e-01f, -9.569403529e-01f}, /* k = 93 */ \
+  {1.950903237e-01f, -9.807852507e-01f}, /* k = 94 */ \
+  {9.801714122e-02f, -9.951847196e-01f}, /* k = 95 */ \
+  {0.000000000e+00f, -1.000000000e+00f}, /* k = 96 */ \
+  {-9.801714122e-02f, -9.951847196e-01f}, /* k = 97 */ \
+  {-1.950903237e-01f, -9.807852507e-01f}, /* k = 98 */ \
+  {-2.902846634e-01f, -9.569403529e-01f}, /* k = 99 */ \
+  {-3.826834261e-01f, -9.238795042e-01f}, /* k = 100 */ \
+  {-4.713967443e-01f, -8.819212914e-01f}, /* k = 101 */ \
+  {-5.555702448e-01f, -8.314695954e-01f}, /* k = 102 */ \
+  {-6.343932748e-01f, -7.730104327e-01f}, /* k = 103 */ \
+  {-7.071067691e-01f, -7.071067691e-01f}, /* k = 104 */ \
+  {-7.730104327e-01f, -6.343932748e-01f}, /* k = 105 */ \
+  {-8.314695954e-01f, -5.555702448e-01f}, /* k = 106 */ \
+  {-8.819212914e-01f, -4.713967443e-01f}, /* k = 107 */ \
+  {-9.238795042e-01f, -3.826834261e-01f}, /* k = 108 */ \
+  {-9.569403529e-01f, -2.902846634e-01f}, /* k = 109 */ \
+  {-9.807852507e-01f, -1.950903237e-01f}, /* k = 110 */ \
+  {-9.951847196e-01f, -9.801714122e-02f}, /* k = 111 */ \
+  {-1.000000000e+00f, 0.000000000e+00f}, /* k = 112 */ \
+  {-9.951847196e-01f, 9.801714122e-02f}, /* k = 113 */ \
+  {-9.807852507e-01f, 1.950903237e-01f}, /* k = 114 */ \
+  {-9.569403529e-01f, 2.902846634e-01f}, /* k = 115 */ \
+  {-9.238795042e-01f, 3.826834261e-01f}, /* k = 116 */ \
+  {-8.819212914e-01f, 4.713967443e-01f}, /* k = 117 */ \
+  {-8.314695954e-01f, 5.555702448e-01f}, /* k = 118 */ \
+  {-7.730104327e-01f, 6.343932748e-01f}, /* k = 119 */ \
+  {-7.071067691e-01f, 7.071067691e-01f}, /* k = 120 */ \
+  {-6.343932748e-01f, 7.730104327e-01f}, /* k = 121 */ \
+  {-5.555702448e-01f, 8.314695954e-01f}, /* k = 122 */ \
+  {-4.713967443e-01f, 8.819212914e-01f}, /* k = 123 */ \
+  {-3.826834261e-01f, 9.238795042e-01f}, /* k = 124 */ \
+  {-2.902846634e-01f, 9.569403529e-01f}, /* k = 125 */ \
+  {-1.950903237e-01f, 9.807852507e-01f}, /* k = 126 */ \
+  {-9.801714122e-02f, 9.951847196e-01f}, /* k = 127 */ \
 }
 
-// sin(pi t) and cos(pi t) for t in [0, 2] from that table: t = k/32 + r with
-// k = rint(32 t), where r = t - k/32 is exact and |r| <= 1/64; sin and cos of
-// x = pi r (|x| <= pi/64) by x - x^3/6 and 1 - x^2/2 + x^4/24 (truncation
-// below 2.4e-9 and 2e-11), then the angle-sum formulas. About 16
-// instructions and one 8-byte load against sincospi_poly's ~28, and within
-// 1e-7 of the exact value over [0, 2] (tests/test_sincospi_host.py).
+// The bits of a float (bit cast, host and device).
+NMG_HD int float_bits(float f) {
+#ifdef __CUDA_ARCH__
+  return __float_as_int(f);
+#else
+  int i;
+  memcpy(&i, &f, sizeof(i));
+  return i;
+#endif
+}
+
+// sin(pi t) and cos(pi t) from that table: t = k/32 + r with k the integer
+// nearest 32 t, where r = t - k/32 is exact and |r| <= 1/64; sin and cos of
+// pi r by r (pi - (pi^3/6) r^2) and 1 + r^2 (-pi^2/2 + (pi^4/24) r^2)
+// (truncation below 2.4e-9 and 2e-11), then the angle-sum formulas. The
+// rounding to k adds 1.5 * 2^23 (so the sum's last mantissa bits hold k,
+// ties to even like rint) and subtracts it again: no conversion
+// instructions, and the table index is those bits modulo 128 -- in range
+// for any t, exact for |t| < 2^17 (t of the mixture lies in [0, 2]). About
+// 15 instructions and one 8-byte load against sincospi_poly's ~28, and
+// within 1e-7 of the exact value over [0, 2] (tests/test_sincospi_host.py).
 NMG_HD void sincospi_tab(const float2* tab, float t, float* s, float* c) {
-  const float kf = rintf(32.f * t);
-  int k = int(kf);
-  k = k < 0 ? 0 : (k > 64 ? 64 : k);
-  const float x = fmaf(kf, -1.f / 32.f, t) * NMG_PI, x2 = x * x;
-  const float sr = fmaf(x * x2, -1.f / 6.f, x);
-  const float cr = fmaf(x2, fmaf(x2, 1.f / 24.f, -0.5f), 1.f);
-  const float2 a = tab[k];
+  constexpr float kRound = 12582912.f;  // 1.5 * 2^23
+  const float y = fmaf(t, 32.f, kRound);
+  const float kf = y - kRound;
+  const float r = fmaf(kf, -1.f / 32.f, t), r2 = r * r;
+  const float sr = r * fmaf(r2, -5.16771278f, 3.14159265f);  // pi^3/6, pi
+  const float cr = fmaf(r2, fmaf(r2, 4.05871213f, -4.93480220f), 1.f);  // pi^4/24, pi^2/2
+  const float2 a = tab[float_bits(y) & 127];
   *s = fmaf(a.x, cr, a.y * sr);
   *c = fmaf(a.y, cr, -(a.x * sr));
 }
@@ -165,10 +246,10 @@ NMG_HD void sincospi_tab(const float2* tab, float t, float* s, float* c) {
 // warp's 32 different indices into constant memory would serialise).
 // A kernel that evaluates angles with kAngTab calls sincospi_tab_fill() once
 // at its start, before any thread can leave.
-static __constant__ float2 c_sincospi32[65] = NMG_SINCOSPI32_TABLE;
-static __shared__ float2 s_sincospi32[65];
+static __constant__ float2 c_sincospi32[128] = NMG_SINCOSPI32_TABLE;
+static __shared__ float2 s_sincospi32[128];
 NMG_D void sincospi_tab_fill() {
-  for (int i = threadIdx.x; i < 65; i += blockDim.x) s_sincospi32[i] = c_sincospi32[i];
+  for (int i = threadIdx.x; i < 128; i += blockDim.x) s_sincospi32[i] = c_sincospi32[i];
   __syncthreads();
 }
 
@@ -387,6 +468,21 @@ template <int K> NMG_D int mix_select(const Mix<K>& m, float u) {
 
 template <bool FAST> NMG_D f3 vmf_sample_dir(float k, f3 mu, float u0, float u1);
 
+// raytracing.h:35-49 Frame(mu) applied to a direction in the lobe's local
+// frame: T = normalize(mu x e), e the branchless axis pick
+// (getPerpendicular, math_utils.h:141-151); B = normalize(mu x T).
+template <bool FAST>
+NMG_D f3 to_frame(f3 mu, f3 loc) {
+  float ax = fabsf(mu.x), ay = fabsf(mu.y), az = fabsf(mu.z);
+  unsigned xm = ((ax - ay) < 0.f) & ((ax - az) < 0.f);
+  unsigned ym = (1u ^ xm) & ((ay - az) < 0.f);
+  unsigned zm = 1u ^ (xm | ym);
+  f3 t = unit3<FAST>(cross3(mu, f3{float(xm), float(ym), float(zm)}));
+  f3 b = unit3<FAST>(cross3(mu, t));
+  return f3{t.x * loc.x + b.x * loc.y + mu.x * loc.z, t.y * loc.x + b.y * loc.y + mu.y * loc.z,
+            t.z * loc.x + b.z * loc.y + mu.z * loc.z};
+}
+
 // vmf.h:48-71: sample lobe `sel` with two uniforms, rotated by the frame of
 // its mean (raytracing.h:35-49, getPerpendicular math_utils.h:141-151).
 template <int K, bool FAST>
@@ -432,15 +528,7 @@ NMG_D f3 vmf_sample_dir(float k, f3 mu, float u0, float u1) {
   xsincos_turn<FAST>(u1, &sp, &cp);
   loc = f3{cp * st, sp * st, ct};
   }
-  // Frame(mu): T = normalize(mu x e), e the branchless axis pick; B = normalize(mu x T)
-  float ax = fabsf(mu.x), ay = fabsf(mu.y), az = fabsf(mu.z);
-  unsigned xm = ((ax - ay) < 0.f) & ((ax - az) < 0.f);
-  unsigned ym = (1u ^ xm) & ((ay - az) < 0.f);
-  unsigned zm = 1u ^ (xm | ym);
-  f3 t = unit3<FAST>(cross3(mu, f3{float(xm), float(ym), float(zm)}));
-  f3 b = unit3<FAST>(cross3(mu, t));
-  return f3{t.x * loc.x + b.x * loc.y + mu.x * loc.z, t.y * loc.x + b.y * loc.y + mu.y * loc.z,
-            t.z * loc.x + b.z * loc.y + mu.z * loc.z};
+  return to_frame<FAST>(mu, loc);
 }
 
 // distribution.h:113-119 with vmf.h:22-27: mixture pdf at unit direction wi.
@@ -455,6 +543,125 @@ NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
     p += m.w[i] * v;
   }
   return p;
+}
+
+// ---------------------------------------------------------------------------
+// The mixture-only kernels' form (raw outputs in memory, no cosine lobe,
+// hardware exponentials and divides, table sin/cos of the lobe angles):
+// only what selection, sampling and the pdf need, with the concentration-
+// dependent branches of the general form evaluated branch-free. The lobe
+// selection is the general form's, operation for operation.
+
+// B(x) = x / (1 - e^{-x}) for 0 <= x < 0.5 from its series
+// 1 + x/2 + x^2/12 - x^4/720 + x^6/30240 (the Bernoulli numbers; the first
+// omitted term, x^8/1209600, is below 3.3e-9 at x = 0.5).
+NMG_HD float bernoulli_gen(float x) {
+  const float x2 = x * x;
+  return fmaf(x2, fmaf(x2, fmaf(x2, 1.f / 30240.f, -1.f / 720.f), 1.f / 12.f), fmaf(0.5f, x, 1.f));
+}
+
+// vMF normaliser k / (2 pi (1 - e^{-2k})) (vmf.h:25-26): (1/4pi) B(2k) below
+// 2k = 0.5, where 1 - e^{-2k} cancels, k/(2pi) / (1 - e^{-2k}) above. Both
+// are evaluated and one selected, so a warp whose lobes fall on both sides
+// does not run two paths in turn. k = 0 gives 1/4pi exactly.
+NMG_D float vmf_norm_sel(float k) {
+  const float x = 2.f * k;
+  const float lo = NMG_INV_4PI * bernoulli_gen(x);
+  const float hi = __fdividef(k * NMG_INV_2PI, 1.f - __expf(-x));
+  return x < 0.5f ? lo : hi;
+}
+
+template <int K> struct MixLean {
+  float lam[K];  // activated lambda
+  float kap[K];  // concentration; 0 for a lobe below M_EPSILON (uniform, vmf.h:24)
+  float ln[K];   // lambda times the lobe's vMF normaliser
+  f3 mu[K];      // unit mean direction
+  float total;   // sum of lambda
+};
+
+// distribution.h:85-98 for the mixture-only kernels (a kernel using it calls
+// sincospi_tab_fill() first). A lobe below M_EPSILON gets kappa 0: its pdf
+// term e^{0} times 1/4pi is the reference's uniform value exactly.
+template <int K>
+NMG_D void mix_activate_lean(MixLean<K>& m, const float* raw, int kappa_softplus) {
+  m.total = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float4 r = reinterpret_cast<const float4*>(raw)[i];
+    m.lam[i] = __expf(act_exp_clamp(r.x));
+    float k = kappa_softplus ? softplus<true>(r.y) : __expf(act_exp_clamp(r.y));
+    k = k < NMG_EPS ? 0.f : k;
+    m.kap[i] = k;
+    float st, ct, sp, cp;
+    lobe_angles<true, kAngTab>(logistic<true>(r.z), logistic<true>(r.w), &st, &ct, &sp, &cp);
+    m.mu[i] = f3{st * cp, st * sp, ct};
+    m.ln[i] = m.lam[i] * vmf_norm_sel(k);
+    m.total += m.lam[i];
+  }
+}
+
+// distribution.h:132-140 (mix_select's arithmetic) that also picks the chosen
+// lobe's concentration and mean; returns the lobe, and 1/total in *inv.
+template <int K>
+NMG_D int mix_select_lean(const MixLean<K>& m, float u, float* k, f3* mu, float* inv) {
+  const float iv = 1.f / m.total;
+  int sel = -1;
+  *k = m.kap[0];
+  *mu = m.mu[0];
+#pragma unroll
+  for (int i = 0; i < K; ++i) {
+    const float w = m.lam[i] * iv;
+    if (sel < 0) {
+      if (u < w) {
+        sel = i;
+        *k = m.kap[i];
+        *mu = m.mu[i];
+      } else {
+        u -= w;
+      }
+    }
+  }
+  *inv = iv;
+  return sel < 0 ? 0 : sel;
+}
+
+// Sum over the lobes of lambda * vMF(wi) (distribution.h:113-119 times the
+// total): the pdf is this over m.total.
+template <int K>
+NMG_D float mix_pdf_lean_sum(const MixLean<K>& m, f3 wi) {
+  float p = 0.f;
+#pragma unroll
+  for (int i = 0; i < K; ++i) p = fmaf(m.ln[i], __expf(m.kap[i] * fminf(0.f, dot3(wi, m.mu[i]) - 1.f)), p);
+  return p;
+}
+
+// vmf.h:48-71 for one lobe (kappa k, 0 for uniform; unit mean mu) with one
+// logarithm: 1 - cos(theta) <= 1 exactly when u0 <= 1 / (1 + e^{-k}), so
+// the side is known before the logarithm. Near the mean,
+// 1 - cos = -log1p(-u0 (1 - e^{-2k})) / k; on the far side,
+// 1 + cos = log1p((1 - u0) (1 - e^{-2k}) / e^{-2k}) / k (= the expm1(2k)
+// form of vmf_sample_dir); 1 - e^{-2k} is 2k / B(2k) below 2k = 0.5.
+NMG_D f3 vmf_sample_lean(float k, f3 mu, float u0, float u1) {
+  float sp, cp;
+  xsincos_turn<true>(u1, &sp, &cp);
+  f3 loc;
+  if (k == 0.f) {  // render/sampling.h:32-37
+    const float z = 1.f - 2.f * u0;
+    const float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+    loc = f3{r * cp, r * sp, z};
+  } else {
+    const float em = __expf(-k), e2 = em * em;
+    const float x = 2.f * k;
+    const float den = x < 0.5f ? __fdividef(x, bernoulli_gen(x)) : 1.f - e2;
+    const bool near = u0 * (1.f + em) <= 1.f;
+    const float a = near ? -u0 * den : (1.f - u0) * __fdividef(den, e2);
+    const float v = log1pf(a) / k;
+    const float om = near ? -v : v;  // 1 - cos near the mean, 1 + cos on the far side
+    const float ct = near ? 1.f - om : om - 1.f;
+    const float st = sqrtf(fmaxf(0.f, om * (2.f - om)));
+    loc = f3{cp * st, sp * st, ct};
+  }
+  return to_frame<true>(mu, loc);
 }
 
 // Raw outputs of lobe i, from memory (16-byte aligned) or from registers.

@@ -86,9 +86,23 @@ NMG_D void stage_sample_row(float4* dst, const float* raw, int stride, const flo
   cp_async_commit();
 }
 
-template <int K, bool FAST>
+// COS: with the cosine-lobe product (cosn given); without it the query takes
+// the lean form (mix_activate_lean and its selection, sampler and pdf).
+template <int K, bool FAST, bool COS>
 NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int kappa_softplus, float* dir,
                       float* pdf, int* lobe) {
+  if constexpr (FAST && !COS) {
+    MixLean<K> m;
+    mix_activate_lean<K>(m, row, kappa_softplus);
+    float k, inv;
+    f3 mu;
+    const int sel = mix_select_lean<K>(m, u.y, &k, &mu, &inv);
+    const f3 d = vmf_sample_lean(k, mu, u.z, u.w);
+    store3(dir, q, d);
+    pdf[q] = mix_pdf_lean_sum<K>(m, d) * inv;
+    if (lobe) lobe[q] = sel;
+    return;
+  }
   Mix<K> m;
   mix_activate<K, FAST, kAngTab>(m, row, kappa_softplus);
   if (cosn) mix_apply_cosine<K, FAST>(m, load3(cosn, q));
@@ -106,7 +120,7 @@ NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int
 // staging takes 36 KB per block, so 6 blocks fill the SM's shared memory, and
 // the 80 registers per thread this caps the kernel at (the unstaged kernel's
 // count) leave room for exactly those 6.
-template <int K, bool FAST, bool STAGED>
+template <int K, bool FAST, bool STAGED, bool COS>
 __global__ void __launch_bounds__(kThreads, STAGED ? 6 : 1) k_mixture_sample(const float* __restrict__ raw, int stride,
                                                              const float* __restrict__ u4,
                                                              const float* __restrict__ cosn, int n,
@@ -124,12 +138,13 @@ __global__ void __launch_bounds__(kThreads, STAGED ? 6 : 1) k_mixture_sample(con
       stage_sample_row<K>(mine + (s ^ 1) * kStage, raw, stride, u4, q + step, n);
       cp_async_wait<1>();  // this thread's copies for query q have landed
       const float4* row = mine + s * kStage;
-      sample_one<K, FAST>(reinterpret_cast<const float*>(row), row[K], cosn, q, kappa_softplus, dir, pdf, lobe);
+      sample_one<K, FAST, COS>(reinterpret_cast<const float*>(row), row[K], cosn, q, kappa_softplus, dir, pdf,
+                               lobe);
     }
     cp_async_wait<0>();
   } else {
     for (; q < n; q += step)
-      sample_one<K, FAST>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
+      sample_one<K, FAST, COS>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
                           pdf, lobe);
   }
 }
@@ -249,8 +264,10 @@ NMG_D void stage_pdf_row(float4* dst, const float* raw, int stride, const float*
 }
 
 // STAGED: as the loss kernel, half rows and directions through shared memory
-// (2 x kThreads x (KH + 1) float4), one wave of resident blocks.
-template <int K, bool FAST, bool STAGED = false>
+// (2 x kThreads x (KH + 1) float4), one wave of resident blocks. COS: with the
+// cosine-lobe product; without it each lane sums lambda * vMF of its lobes in
+// the lean form and the pdf is the pair's sum over the pair's total.
+template <int K, bool FAST, bool STAGED, bool COS>
 __global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restrict__ raw, int stride,
                                                            const float* __restrict__ wi,
                                                            const float* __restrict__ cosn, int n,
@@ -265,18 +282,28 @@ __global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restri
   if constexpr (STAGED) stage_pdf_row<KH>(mine, raw, stride, wi, t, n, h);
   for (int sb = 0; (t >> 1) < n; t += step, sb ^= 1) {
     const long q = t >> 1;
-    Mix<KH> m;
-    float p;
+    const float* half_row;
+    f3 w;
     if constexpr (STAGED) {
       stage_pdf_row<KH>(mine + (sb ^ 1) * kStage, raw, stride, wi, t + step, n, h);
       cp_async_wait<1>();  // this lane's copies for query q have landed
       const float4* st4 = mine + sb * kStage;
-      pair_mixture<K, FAST>(m, reinterpret_cast<const float*>(st4), cosn, q, kappa_softplus);
-      const float4 w = st4[KH];
-      p = pair_sum(mix_pdf<KH, FAST>(m, f3{w.x, w.y, w.z}));
+      half_row = reinterpret_cast<const float*>(st4);
+      const float4 w4 = st4[KH];
+      w = f3{w4.x, w4.y, w4.z};
     } else {
-      pair_mixture<K, FAST>(m, raw + q * stride + h * KH * 4, cosn, q, kappa_softplus);
-      p = pair_sum(mix_pdf<KH, FAST>(m, load3(wi, q)));
+      half_row = raw + q * stride + h * KH * 4;
+      w = load3(wi, q);
+    }
+    float p;
+    if constexpr (FAST && !COS) {
+      MixLean<KH> m;
+      mix_activate_lean<KH>(m, half_row, kappa_softplus);
+      p = pair_sum(mix_pdf_lean_sum<KH>(m, w)) / pair_sum(m.total);
+    } else {
+      Mix<KH> m;
+      pair_mixture<K, FAST>(m, half_row, cosn, q, kappa_softplus);
+      p = pair_sum(mix_pdf<KH, FAST>(m, w));
     }
     if (h == 0) pdf[q] = p;
   }
@@ -366,8 +393,9 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       cc[i] = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
       dta[i] = cth * (wi.x * cph + wi.y * sph) - wi.z * sth;
       dpa[i] = (wi.y * cph - wi.x * sph) * sth;
-      const float k = kap[i];
-      vmf[i] = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, cc[i] - 1.f)) * vmf_norm<FAST>(k);
+      // below M_EPSILON the lobe is uniform (vmf.h:24): kappa 0 gives e^{0} / 4pi without a branch
+      const float kz = kap[i] < NMG_EPS ? 0.f : kap[i];
+      vmf[i] = xexp<FAST>(kz * fminf(0.f, cc[i] - 1.f)) * vmf_norm_sel(kz);
       lt += lam[i];
       nt += lam[i] * vmf[i];
     }
@@ -391,15 +419,13 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
     for (int i = 0; i < KH; ++i) {
       const float k = kap[i];
       const float wv = (lam[i] * inv_total) * vmf[i];
-      float ik;
-      if (o.kappa_poly && k < 1.f) {
-        ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
-      } else if (!o.kappa_poly && k < 1e-2f) {
-        ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
-      } else {
-        const float e = xexp<FAST>(-2.f * k);
-        ik = xdiv<FAST>(1.f, k) - xdiv<FAST>(1.f + e, 1.f - e);
-      }
+      // d log(vMF normaliser) / d kappa (distribution.h:160-172): the polynomial below kappa 1 or the
+      // series below 1e-2, else 1/k - coth(k); both forms evaluated and one selected (no divergence)
+      const float e = xexp<FAST>(-2.f * k);
+      const float ik_exact = xdiv<FAST>(1.f, k) - xdiv<FAST>(1.f + e, 1.f - e);
+      const float ik_small = o.kappa_poly ? 0.000926f + -0.344883f * k + 0.030147f * (k * k)
+                                          : k * (-1.f / 3.f + k * k * (1.f / 45.f));
+      const float ik = k < (o.kappa_poly ? 1.f : 1e-2f) ? ik_small : ik_exact;
       float g0 = prefix * ((vmf[i] - qv) * inv_total * sel) * lam[i];
       float g1 = prefix * (wv * (cc[i] + ik) * sel) * dkap[i];
       float g2 = prefix * (wv * k * dta[i] * sel) * NMG_PI * (sgt[i] * (1.f - sgt[i]));
@@ -432,9 +458,15 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
   constexpr bool staged = stage_fits(per_thread);
   const int smem = staged ? 2 * kThreads * per_thread : 0;
   int grid = grid_for(n);
-  if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true>, smem, n);
-  k_mixture_sample<K, kMixFast, staged><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, cosn, n,
-                                                                     o->kappa_softplus, dir, pdf, lobe);
+  if (cosn) {
+    if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true, true>, smem, n);
+    k_mixture_sample<K, kMixFast, staged, true><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, cosn, n,
+                                                                             o->kappa_softplus, dir, pdf, lobe);
+  } else {
+    if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true, false>, smem, n);
+    k_mixture_sample<K, kMixFast, staged, false><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, nullptr, n,
+                                                                              o->kappa_softplus, dir, pdf, lobe);
+  }
   return check_launch("nmg_mixture_sample");
 }
 
@@ -444,9 +476,15 @@ static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const 
   if constexpr (K % 2 == 0) {
     constexpr int smem = 2 * kThreads * (K / 2 + 1) * 16;
     static_assert(stage_fits((K / 2 + 1) * 16), "pdf staging above 48 KB");
-    const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true>, smem, 2L * n);
-    k_mixture_pdf2<K, kMixFast, true><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus,
-                                                                    pdf);
+    if (cosn) {
+      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true, true>, smem, 2L * n);
+      k_mixture_pdf2<K, kMixFast, true, true><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, cosn, n,
+                                                                            o->kappa_softplus, pdf);
+    } else {
+      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true, false>, smem, 2L * n);
+      k_mixture_pdf2<K, kMixFast, true, false><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, nullptr, n,
+                                                                             o->kappa_softplus, pdf);
+    }
   }
   else
     k_mixture_pdf<K, kMixFast><<<grid_for(n), kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus, pdf);

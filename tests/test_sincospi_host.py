@@ -4,7 +4,7 @@ and sincospi_tab).
 The mixture kernels evaluate sin(pi t) and cos(pi t) of the logistic lobe
 angles with their own functions instead of the hardware approximation: the
 plain FP32 path with a folded polynomial, the mixture-only kernels from a
-65-entry table of sin/cos(pi k/32) and short polynomials of the remainder.
+128-entry table of sin/cos(pi k/32) and short polynomials of the remainder.
 An error e in a lobe mean becomes a relative pdf error of about e * kappa,
 so both must stay within ~1e-7 of the exact value. The functions are
 __host__ __device__, so this test compiles a small host program against the
@@ -28,7 +28,7 @@ PROGRAM = r"""
 int main() {
   const long n = 2000000;
   const long double pi = 3.141592653589793238462643383279502884L;
-  static const float2 tab[65] = NMG_SINCOSPI32_TABLE;
+  static const float2 tab[128] = NMG_SINCOSPI32_TABLE;
   double e2 = 0.0, e1 = 0.0, et = 0.0;
   for (long i = 0; i <= n; ++i) {
     // t over [0, 2] (the azimuth argument 2 sp) and over [0, 1] (theta's)
@@ -48,7 +48,7 @@ int main() {
     e1 = fmax(e1, double(fabsl((long double)c - cosl(x))));
   }
   double ee = 0.0;  // the table entries themselves
-  for (int k = 0; k <= 64; ++k) {
+  for (int k = 0; k < 128; ++k) {
     const long double x = pi * (long double)k / 32.0L;
     ee = fmax(ee, double(fabsl((long double)tab[k].x - sinl(x))));
     ee = fmax(ee, double(fabsl((long double)tab[k].y - cosl(x))));
