@@ -43,9 +43,8 @@ static int grid_for(long n) {
   return int(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
 }
 
-// One wave of the blocks that fit on the device at once (a persistent grid:
-// the staged kernels overlap each thread's next copies with its current
-// query, which pays only over many queries per thread), or fewer for small n.
+// One wave of the blocks that fit on the device at once (the kernels loop
+// over the queries with a grid stride), or fewer for small n.
 template <class Kern>
 static int resident_grid(Kern kernel, int smem, long n) {
   int dev = 0, sms = 152, per_sm = 1;
@@ -54,36 +53,6 @@ static int resident_grid(Kern kernel, int smem, long n) {
     per_sm = 1;
   const long blocks = (n + kThreads - 1) / kThreads, cap = long(sms) * per_sm;
   return int(blocks < cap ? (blocks > 0 ? blocks : 1) : cap);
-}
-
-// Per-thread asynchronous copies global -> shared (cp.async, bypassing L1):
-// a thread stages the rows of its next query while it computes the current
-// one, and waits only for its own copies (cp.async.wait_group), so no block
-// barrier and no spin-wait is involved.
-NMG_D uint32_t shared_u32(const void* p) { return static_cast<uint32_t>(__cvta_generic_to_shared(p)); }
-NMG_D void cp_async16(void* smem, const void* gmem) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(shared_u32(smem)), "l"(gmem) : "memory");
-}
-NMG_D void cp_async4(void* smem, const void* gmem) {
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(shared_u32(smem)), "l"(gmem) : "memory");
-}
-NMG_D void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N> NMG_D void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-// Double-buffered staging fits the 48 KB of dynamic shared memory a launch
-// gets without opting in: 2 x 128 threads x `per_thread` bytes.
-constexpr bool stage_fits(int per_thread) { return 2 * kThreads * per_thread <= 48 * 1024; }
-
-// Raw row (K float4) and uniforms (one float4) of query q into `dst`, as one
-// commit group (empty past the end, so that the group count stays uniform).
-template <int K>
-NMG_D void stage_sample_row(float4* dst, const float* raw, int stride, const float* u4, long q, int n) {
-  if (q < n) {
-#pragma unroll
-    for (int i = 0; i < K; ++i) cp_async16(dst + i, raw + q * stride + 4 * i);
-    cp_async16(dst + K, u4 + 4 * q);
-  }
-  cp_async_commit();
 }
 
 // COS: with the cosine-lobe product (cosn given); without it the query takes
@@ -113,40 +82,27 @@ NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int
   if (lobe) lobe[q] = sel;
 }
 
-// STAGED: rows pass through shared memory (dynamic, 2 x kThreads x (K + 1)
-// float4), the next query's copies in flight during the current query's
-// arithmetic; otherwise direct 128-bit loads (K = 16, whose staging would
-// need more than 48 KB). Staged, 6 blocks per SM are asked for: at K = 8 the
-// staging takes 36 KB per block, so 6 blocks fill the SM's shared memory, and
-// the 80 registers per thread this caps the kernel at (the unstaged kernel's
-// count) leave room for exactly those 6.
-template <int K, bool FAST, bool STAGED, bool COS>
-__global__ void __launch_bounds__(kThreads, STAGED ? 6 : 1) k_mixture_sample(const float* __restrict__ raw, int stride,
-                                                             const float* __restrict__ u4,
-                                                             const float* __restrict__ cosn, int n,
-                                                             int kappa_softplus, float* __restrict__ dir,
-                                                             float* __restrict__ pdf, int* __restrict__ lobe) {
+// Direct 128-bit loads of each query's row and uniforms, one wave of
+// resident blocks (a grid-stride loop). At K <= 8 the bound of 5 blocks per
+// SM lets the lean form keep its lobes in 96 registers without spilling;
+// 2,097,152 queries at K = 8 measured 98 us this way against 115 us with the
+// rows staged in shared memory by per-thread cp.async copies (6 blocks per
+// SM at 80 registers, the staging filling the SM's shared memory) and
+// 108 us with 106 registers and 4 blocks.
+template <int K, bool FAST, bool COS>
+__global__ void __launch_bounds__(kThreads, K <= 8 ? 5 : 1) k_mixture_sample(const float* __restrict__ raw,
+                                                                             int stride,
+                                                                             const float* __restrict__ u4,
+                                                                             const float* __restrict__ cosn, int n,
+                                                                             int kappa_softplus,
+                                                                             float* __restrict__ dir,
+                                                                             float* __restrict__ pdf,
+                                                                             int* __restrict__ lobe) {
   sincospi_tab_fill();
   const long step = long(gridDim.x) * blockDim.x;
-  long q = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  if constexpr (STAGED) {
-    constexpr int R = K + 1, kStage = kThreads * R;
-    extern __shared__ float4 s_stage[];
-    float4* mine = s_stage + threadIdx.x * R;
-    stage_sample_row<K>(mine, raw, stride, u4, q, n);
-    for (int s = 0; q < n; q += step, s ^= 1) {
-      stage_sample_row<K>(mine + (s ^ 1) * kStage, raw, stride, u4, q + step, n);
-      cp_async_wait<1>();  // this thread's copies for query q have landed
-      const float4* row = mine + s * kStage;
-      sample_one<K, FAST, COS>(reinterpret_cast<const float*>(row), row[K], cosn, q, kappa_softplus, dir, pdf,
-                               lobe);
-    }
-    cp_async_wait<0>();
-  } else {
-    for (; q < n; q += step)
-      sample_one<K, FAST, COS>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
-                          pdf, lobe);
-  }
+  for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += step)
+    sample_one<K, FAST, COS>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
+                             pdf, lobe);
 }
 
 template <int K, bool FAST>
@@ -248,53 +204,24 @@ NMG_D void pair_mixture(Mix<K / 2>& m, const float* half_row, const float* cosn,
   }
 }
 
-// Lane h's half row (KH float4) and the direction (3 floats, 4-byte copies)
-// of the query of thread index t, as one commit group (empty past the end).
-template <int KH>
-NMG_D void stage_pdf_row(float4* dst, const float* raw, int stride, const float* wi, long t, int n, int h) {
-  const long q = t >> 1;
-  if (q < n) {
-#pragma unroll
-    for (int i = 0; i < KH; ++i) cp_async16(dst + i, raw + q * stride + h * KH * 4 + 4 * i);
-    float* wd = reinterpret_cast<float*>(dst + KH);
-#pragma unroll
-    for (int j = 0; j < 3; ++j) cp_async4(wd + j, wi + 3 * q + j);
-  }
-  cp_async_commit();
-}
-
-// STAGED: as the loss kernel, half rows and directions through shared memory
-// (2 x kThreads x (KH + 1) float4), one wave of resident blocks. COS: with the
-// cosine-lobe product; without it each lane sums lambda * vMF of its lobes in
-// the lean form and the pdf is the pair's sum over the pair's total.
-template <int K, bool FAST, bool STAGED, bool COS>
-__global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restrict__ raw, int stride,
-                                                           const float* __restrict__ wi,
-                                                           const float* __restrict__ cosn, int n,
-                                                           int kappa_softplus, float* __restrict__ pdf) {
-  constexpr int KH = K / 2, R = KH + 1, kStage = kThreads * R;
+// Direct loads, one wave of resident blocks. COS: with the cosine-lobe
+// product; without it each lane sums lambda * vMF of its lobes in the lean
+// form and the pdf is the pair's sum over the pair's total. 8 blocks per SM
+// at K <= 8 (56 registers): 70 us for 2,097,152 queries at K = 8, against
+// 80 us with the rows staged in shared memory by per-thread cp.async copies.
+template <int K, bool FAST, bool COS>
+__global__ void __launch_bounds__(kThreads, K <= 8 ? 8 : 1) k_mixture_pdf2(const float* __restrict__ raw, int stride,
+                                                                         const float* __restrict__ wi,
+                                                                         const float* __restrict__ cosn, int n,
+                                                                         int kappa_softplus, float* __restrict__ pdf) {
+  constexpr int KH = K / 2;
   const int h = threadIdx.x & 1;
   sincospi_tab_fill();
   const long step = long(gridDim.x) * blockDim.x;
-  long t = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  extern __shared__ float4 s_stage[];
-  float4* mine = s_stage + threadIdx.x * R;
-  if constexpr (STAGED) stage_pdf_row<KH>(mine, raw, stride, wi, t, n, h);
-  for (int sb = 0; (t >> 1) < n; t += step, sb ^= 1) {
+  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += step) {
     const long q = t >> 1;
-    const float* half_row;
-    f3 w;
-    if constexpr (STAGED) {
-      stage_pdf_row<KH>(mine + (sb ^ 1) * kStage, raw, stride, wi, t + step, n, h);
-      cp_async_wait<1>();  // this lane's copies for query q have landed
-      const float4* st4 = mine + sb * kStage;
-      half_row = reinterpret_cast<const float*>(st4);
-      const float4 w4 = st4[KH];
-      w = f3{w4.x, w4.y, w4.z};
-    } else {
-      half_row = raw + q * stride + h * KH * 4;
-      w = load3(wi, q);
-    }
+    const float* half_row = raw + q * stride + h * KH * 4;
+    const f3 w = load3(wi, q);
     float p;
     if constexpr (FAST && !COS) {
       MixLean<KH> m;
@@ -307,68 +234,34 @@ __global__ void __launch_bounds__(kThreads) k_mixture_pdf2(const float* __restri
     }
     if (h == 0) pdf[q] = p;
   }
-  if constexpr (STAGED) cp_async_wait<0>();
-}
-
-// Lane h's half row (KH float4) and the whole record (up to 8 floats, 4-byte
-// copies: records are 24 or 28 bytes) of the query of thread index t, as one
-// commit group (empty past the end).
-template <int KH>
-NMG_D void stage_loss_row(float4* dst, const float* raw, int stride, const float* rec, int rstride, long t, int n,
-                          int h) {
-  const long q = t >> 1;
-  if (q < n) {
-#pragma unroll
-    for (int i = 0; i < KH; ++i) cp_async16(dst + i, raw + q * stride + h * KH * 4 + 4 * i);
-    float* rd = reinterpret_cast<float*>(dst + KH);
-#pragma unroll
-    for (int j = 0; j < 8; ++j)
-      if (j < rstride) cp_async4(rd + j, rec + q * rstride + j);
-  }
-  cp_async_commit();
 }
 
 // train.cu:69-172 with the lobes split over a lane pair: each lane computes
 // its lobes' activations, vMF values and gradients; q and the total come
-// from the pair's partial sums.
-// STAGED: each lane's half row and the record pass through shared memory
-// (dynamic, 2 x kThreads x (KH + 2) float4), the next query's copies in
-// flight during the current one's arithmetic (launched as one wave of
-// resident blocks); otherwise direct loads.
-template <int K, bool SEL, bool STAGED = false>
-__global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __restrict__ raw, int stride,
-                                                                 const float* __restrict__ rec, int rstride, int n,
-                                                                 float scale, MixOpts o, float* __restrict__ grad,
-                                                                 float* __restrict__ loss,
-                                                                 double* __restrict__ partials) {
+// from the pair's partial sums. Direct loads; 8 blocks per SM at K <= 8
+// (64 registers): 154 us for 2,097,152 queries at K = 8, against 178 us
+// with the rows staged in shared memory by per-thread cp.async copies and
+// 166 us at the 89 registers the compiler picks unbounded.
+template <int K, bool SEL>
+__global__ void __launch_bounds__(kThreads, K <= 8 ? 8 : 1) k_mixture_loss_grad2(const float* __restrict__ raw,
+                                                                               int stride,
+                                                                               const float* __restrict__ rec,
+                                                                               int rstride, int n, float scale,
+                                                                               MixOpts o, float* __restrict__ grad,
+                                                                               float* __restrict__ loss,
+                                                                               double* __restrict__ partials) {
   constexpr int KH = K / 2;
   constexpr bool FAST = kMixFast;
-  constexpr int R = KH + 2, kStage = kThreads * R;  // float4 per lane: its lobes, the record
   const int h = threadIdx.x & 1;
   sincospi_tab_fill();
   double acc = 0.0;
   const long step = long(gridDim.x) * blockDim.x;
-  long t = long(blockIdx.x) * blockDim.x + threadIdx.x;
-  extern __shared__ float4 s_stage[];
-  float4* mine = s_stage + threadIdx.x * R;
-  if constexpr (STAGED) stage_loss_row<KH>(mine, raw, stride, rec, rstride, t, n, h);
-  for (int sb = 0; (t >> 1) < n; t += step, sb ^= 1) {
+  for (long t = long(blockIdx.x) * blockDim.x + threadIdx.x; (t >> 1) < n; t += step) {
     const long q = t >> 1;
     float r[8];
-    const float* row;
-    if constexpr (STAGED) {
-      stage_loss_row<KH>(mine + (sb ^ 1) * kStage, raw, stride, rec, rstride, t + step, n, h);
-      cp_async_wait<1>();  // this lane's copies for query q have landed
-      const float4* st4 = mine + sb * kStage;
-      row = reinterpret_cast<const float*>(st4);
-      const float* rs = reinterpret_cast<const float*>(st4 + KH);
 #pragma unroll
-      for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rs[j] : 0.f;
-    } else {
-#pragma unroll
-      for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
-      row = raw + q * stride + h * KH * 4;
-    }
+    for (int j = 0; j < 8; ++j) r[j] = j < rstride ? rec[q * rstride + j] : 0.f;
+    const float* row = raw + q * stride + h * KH * 4;
     float swt, cwt, swp, cwp;
     sincosf(r[0], &swt, &cwt);
     sincosf(r[1], &swp, &cwp);
@@ -444,7 +337,6 @@ __global__ void __launch_bounds__(kThreads) k_mixture_loss_grad2(const float* __
       acc += double(l);
     }
   }
-  if constexpr (STAGED) cp_async_wait<0>();
   const double s = block_sum_fixed(acc);
   if (threadIdx.x == 0 && partials) partials[blockIdx.x] = s;
 }
@@ -454,18 +346,14 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
                                 int n, float* dir, float* pdf, int* lobe, cudaStream_t st) {
   // one thread per query: splitting the lobes over a lane pair (as the loss does) measured slower here,
   // the selection and the sampling of the chosen lobe being per-query work both lanes would repeat
-  constexpr int per_thread = (K + 1) * 16;
-  constexpr bool staged = stage_fits(per_thread);
-  const int smem = staged ? 2 * kThreads * per_thread : 0;
-  int grid = grid_for(n);
   if (cosn) {
-    if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true, true>, smem, n);
-    k_mixture_sample<K, kMixFast, staged, true><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, cosn, n,
-                                                                             o->kappa_softplus, dir, pdf, lobe);
+    const int grid = resident_grid(k_mixture_sample<K, kMixFast, true>, 0, n);
+    k_mixture_sample<K, kMixFast, true><<<grid, kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
+                                                                   dir, pdf, lobe);
   } else {
-    if constexpr (staged) grid = resident_grid(k_mixture_sample<K, kMixFast, true, false>, smem, n);
-    k_mixture_sample<K, kMixFast, staged, false><<<grid, kThreads, smem, st>>>(raw, o->stride, u4, nullptr, n,
-                                                                              o->kappa_softplus, dir, pdf, lobe);
+    const int grid = resident_grid(k_mixture_sample<K, kMixFast, false>, 0, n);
+    k_mixture_sample<K, kMixFast, false><<<grid, kThreads, 0, st>>>(raw, o->stride, u4, nullptr, n,
+                                                                    o->kappa_softplus, dir, pdf, lobe);
   }
   return check_launch("nmg_mixture_sample");
 }
@@ -474,16 +362,14 @@ template <int K>
 static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const float* wi, const float* cosn, int n,
                              float* pdf, cudaStream_t st) {
   if constexpr (K % 2 == 0) {
-    constexpr int smem = 2 * kThreads * (K / 2 + 1) * 16;
-    static_assert(stage_fits((K / 2 + 1) * 16), "pdf staging above 48 KB");
     if (cosn) {
-      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true, true>, smem, 2L * n);
-      k_mixture_pdf2<K, kMixFast, true, true><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, cosn, n,
-                                                                            o->kappa_softplus, pdf);
+      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true>, 0, 2L * n);
+      k_mixture_pdf2<K, kMixFast, true><<<grid, kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus,
+                                                                   pdf);
     } else {
-      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, true, false>, smem, 2L * n);
-      k_mixture_pdf2<K, kMixFast, true, false><<<grid, kThreads, smem, st>>>(raw, o->stride, wi, nullptr, n,
-                                                                             o->kappa_softplus, pdf);
+      const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, false>, 0, 2L * n);
+      k_mixture_pdf2<K, kMixFast, false><<<grid, kThreads, 0, st>>>(raw, o->stride, wi, nullptr, n,
+                                                                    o->kappa_softplus, pdf);
     }
   }
   else
@@ -499,17 +385,14 @@ static nmg_status launch_loss(const nmg_mixture_opts* o, const float* raw, const
   int blocks = grid_for(n);  // the workspace holds one partial per block of this grid (at most)
   const float scale = loss_scale / float(n);
   if constexpr (K % 2 == 0) {
-    constexpr int smem = 2 * kThreads * (K / 2 + 2) * 16;
-    static_assert(stage_fits((K / 2 + 2) * 16), "loss staging above 48 KB");
     if (o->selection) {
-      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, true, true>, smem, 2L * n));
-      k_mixture_loss_grad2<K, true, true><<<blocks, kThreads, smem, st>>>(raw, o->stride, rec, rstride, n, scale, mo,
-                                                                         grad, loss, loss_sum ? partials : nullptr);
+      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, true>, 0, 2L * n));
+      k_mixture_loss_grad2<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                 loss, loss_sum ? partials : nullptr);
     } else {
-      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, false, true>, smem, 2L * n));
-      k_mixture_loss_grad2<K, false, true><<<blocks, kThreads, smem, st>>>(raw, o->stride, rec, rstride, n, scale,
-                                                                          mo, grad, loss,
-                                                                          loss_sum ? partials : nullptr);
+      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, false>, 0, 2L * n));
+      k_mixture_loss_grad2<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
+                                                                  loss, loss_sum ? partials : nullptr);
     }
   } else {
     if (o->selection)

@@ -170,6 +170,12 @@ def test_softplus_kappa(nmg, oracle, synth):
     ok = (lbg == lb64) & ~near_switch
     assert ok.mean() > 0.998
     assert np.abs(d.cpu().numpy()[ok] - d64[ok]).max() <= 1e-4
+    # the pdf at the sampled direction, uniform lobes (kappa < 1e-5: 1/4pi) included; kappa <= 6.0025
+    dg = d.cpu().numpy()
+    p64 = oracle.mixture_pdf(raw, 8, dg, fp64=True, o=oracle.opts(kappa_softplus=1))
+    assert np.all(np.abs(p.cpu().numpy() - p64) / p64 <= 1e-4)
+    pw = nmg.mixture_pdf(r, d, 8, kappa_softplus=True).cpu().numpy()
+    assert np.all(np.abs(pw - p64) / p64 <= 1e-4)
     g, _, _ = nmg.mixture_loss_grad(r, rc, 8, kappa_softplus=True)
     g64, _, _ = oracle.mixture_loss_grad(raw, 8, rec, fp64=True, o=oracle.opts(kappa_softplus=1))
     err = np.abs(g.cpu().numpy()[:, :32] - g64[:, :32]).max(axis=1)
