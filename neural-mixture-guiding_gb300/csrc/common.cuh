@@ -41,6 +41,35 @@ NMG_D void store3(float* p, long i, f3 v) {
   p[3 * i + 2] = v.z;
 }
 
+// store3 by a warp whose lane i holds row q0 + i (q0 a multiple of 32).
+// When all 32 lanes arrive together with valid rows and p is 16-byte
+// aligned, the warp's 96 floats go out as 24 float4, each gathered from its
+// owning lanes by shuffles, instead of three 4-byte stores per lane at a
+// 12-byte stride: every 32-byte sector is written whole, with a third of
+// the L2 write requests, and as whole sectors across the host link when p
+// is mapped host memory. Otherwise (a partial last tile, lanes that left
+// after a failed wait) each valid lane stores its own row.
+NMG_D void store3_warp(float* p, long q, f3 v, bool valid) {
+  const unsigned act = __activemask();
+  const unsigned all = __ballot_sync(act, valid);
+  const int lane = threadIdx.x & 31;
+  if (act != 0xffffffffu || all != 0xffffffffu || (reinterpret_cast<uintptr_t>(p) & 15u) != 0u) {
+    if (valid) store3(p, q, v);
+    return;
+  }
+  float o[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int e = 4 * lane + j;      // float e of the warp's 96 (lanes 24..31 gather nothing they store)
+    const int src = (e / 3) & 31, c = e % 3;
+    const float x = __shfl_sync(0xffffffffu, v.x, src);
+    const float y = __shfl_sync(0xffffffffu, v.y, src);
+    const float z = __shfl_sync(0xffffffffu, v.z, src);
+    o[j] = c == 0 ? x : (c == 1 ? y : z);
+  }
+  if (lane < 24) reinterpret_cast<float4*>(p + 3 * (q - lane))[lane] = make_float4(o[0], o[1], o[2], o[3]);
+}
+
 NMG_HD int ceil_div(long a, long b) { return int((a + b - 1) / b); }
 
 }  // namespace nmg

@@ -398,13 +398,13 @@ __global__ void __launch_bounds__(4 * kRows, 1) k_fused_query_pair(const __grid_
     mine[7] = pd;
     ok = bar_red_and(1 + p, 2 * kRows, ok);
     if (!ok) break;
-    if (h == 0 && valid) {
-      a.pdf[q] = pd + other[7];
-      if (!a.wi) {
-        store3(a.dir, q, d);
-        if (a.lobe) a.lobe[q] = sel;
+    if (h == 0) {
+      if (!a.wi) store3_warp(a.dir, q, d, valid);
+      if (valid) {
+        a.pdf[q] = pd + other[7];
+        if (!a.wi && a.lobe) a.lobe[q] = sel;
+        if (a.sel && a.selection) a.sel[q] = logistic<true>(sel_logit);
       }
-      if (a.sel && a.selection) a.sel[q] = logistic<true>(sel_logit);
     }
   }
   if (!ok && t == 0) atomicExch(a.err, 2);

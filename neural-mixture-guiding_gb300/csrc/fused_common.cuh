@@ -327,6 +327,10 @@ NMG_D f3 face_fwd(f3 n, f3 v) { return dot3(n, v) > 0.f ? n : f3{-n.x, -n.y, -n.
 // optional raw row, then (unless raw_mode) the mixture with the optional
 // cosine lobe, and either the sampled direction with its pdf, lobe and
 // selection probability, or (a.wi set) the pdf at the given direction.
+// (The direction is stored per thread here: gathering a warp's directions
+// into whole-sector float4 stores, as the 16-lobe epilogues do, kept three
+// more values live across the pdf and made the 8-lobe consumers spill:
+// query pass 0.647 -> 0.751 ms.)
 template <int K, int NOUTMAX>
 NMG_D void query_epilogue(const FusedArgs& a, long q, const float (&r)[NOUTMAX]) {
   if (a.raw) {
@@ -457,12 +461,12 @@ NMG_D void query_epilogue_streamed(const FusedArgs& a, long q, bool valid, uint3
     tc::tmem_load<1>(lane_addr + 4 * K, v);
     slogit = v[0];
   }
-  if (!valid) return;
   if (a.wi) {
-    a.pdf[q] = p;
+    if (valid) a.pdf[q] = p;
     return;
   }
-  store3(a.dir, q, d);
+  store3_warp(a.dir, q, d, valid);
+  if (!valid) return;
   a.pdf[q] = p;
   if (a.lobe) a.lobe[q] = sel;
   if (a.sel && a.selection) a.sel[q] = logistic<true>(slogit);
