@@ -869,15 +869,27 @@ NMG_D void half_loss_lobes(HalfLoss<KH>& s, const RAW& raw, const float* rec, co
     lobe_angles<FAST, PRECISE, false>(sgt, sgp, &sth, &cth, &sph, &cph);
     const float cc = wi.x * sth * cph + wi.y * sth * sph + wi.z * cth;
     const float k = kap;
-    const float vmf = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, cc - 1.f)) * vmf_norm<FAST>(k);
-    float ik;
-    if (o.kappa_poly && k < 1.f) {
-      ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
-    } else if (!o.kappa_poly && k < 1e-2f) {
-      ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+    float vmf, ik;
+    if (FAST) {
+      // branch-free: kappa below M_EPSILON as 0 (e^{0} / 4pi, the uniform lobe), both forms of
+      // the normaliser and of d log(normaliser) / d kappa evaluated and one selected
+      const float kz = k < NMG_EPS ? 0.f : k;
+      vmf = __expf(kz * fminf(0.f, cc - 1.f)) * vmf_norm_sel(kz);
+      const float e = __expf(-2.f * k);
+      const float ik_exact = 1.f / k - (1.f + e) / (1.f - e);
+      const float ik_small = o.kappa_poly ? 0.000926f + -0.344883f * k + 0.030147f * (k * k)
+                                          : k * (-1.f / 3.f + k * k * (1.f / 45.f));
+      ik = k < (o.kappa_poly ? 1.f : 1e-2f) ? ik_small : ik_exact;
     } else {
-      const float e = xexp<FAST>(-2.f * k);
-      ik = 1.f / k - (1.f + e) / (1.f - e);
+      vmf = k < NMG_EPS ? NMG_INV_4PI : xexp<FAST>(k * fminf(0.f, cc - 1.f)) * vmf_norm<FAST>(k);
+      if (o.kappa_poly && k < 1.f) {
+        ik = 0.000926f + -0.344883f * k + 0.030147f * (k * k);
+      } else if (!o.kappa_poly && k < 1e-2f) {
+        ik = k * (-1.f / 3.f + k * k * (1.f / 45.f));
+      } else {
+        const float e = xexp<FAST>(-2.f * k);
+        ik = 1.f / k - (1.f + e) / (1.f - e);
+      }
     }
     s.lam[i] = lam;
     s.vmf[i] = vmf;
