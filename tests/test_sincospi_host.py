@@ -1,5 +1,6 @@
 """Accuracy of the lobe-mean sine/cosine (csrc/mixture.cuh: sincospi_poly
-and sincospi_tab).
+and sincospi_tab) and of the series of the mixture-only kernels' vMF
+normaliser (bernoulli_gen).
 
 The mixture kernels evaluate sin(pi t) and cos(pi t) of the logistic lobe
 angles with their own functions instead of the hardware approximation: the
@@ -77,3 +78,50 @@ def test_sincospi_poly_and_table_within_1e7(tmp_path):
     assert e_tab <= 1e-7, e_tab
     # every entry rounded correctly: within half an FP32 ulp of values below 1 (2^-25)
     assert e_entry <= 2.0 ** -25, e_entry
+
+
+BERNOULLI = r"""
+#include <cmath>
+#include <cstdio>
+#include "mixture.cuh"
+
+int main() {
+  // B(x) = x / (1 - e^{-x}) on [0, 0.5], the range where the mixture-only
+  // kernels' vMF normaliser takes the series (1/4pi) B(2 kappa)
+  const long n = 1000000;
+  double er = 0.0;
+  for (long i = 0; i <= n; ++i) {
+    const float x = float(0.5 * double(i) / double(n));
+    const long double xl = x;
+    const long double exact = xl > 0 ? xl / -expm1l(-xl) : 1.0L;
+    er = fmax(er, double(fabsl((long double)nmg::bernoulli_gen(x) / exact - 1.0L)));
+  }
+  // the sampler's 1 - e^{-2k} = 2k / B(2k), relative
+  double ed = 0.0;
+  for (long i = 1; i <= n; ++i) {
+    const float x = float(0.5 * double(i) / double(n));
+    const long double exact = -expm1l(-(long double)x);
+    ed = fmax(ed, double(fabsl((long double)(x / nmg::bernoulli_gen(x)) / exact - 1.0L)));
+  }
+  printf("%.6e %.6e\n", er, ed);
+  return 0;
+}
+"""
+
+
+def test_bernoulli_series_within_2e7(tmp_path):
+    """bernoulli_gen (csrc/mixture.cuh) against long double: the normaliser's series below
+    2 kappa = 0.5 and the sampler's 1 - e^{-2 kappa} derived from it, both within 2e-7 relative
+    (a few FP32 roundings; the truncation is below 3.3e-9)."""
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not available")
+    src = tmp_path / "bern.cu"
+    src.write_text(BERNOULLI)
+    exe = tmp_path / "bern"
+    subprocess.run([nvcc, "-std=c++17", "-O2", "-I", CSRC, str(src), "-o", str(exe)], check=True,
+                   capture_output=True, timeout=600)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True, timeout=600).stdout.split()
+    e_series, e_den = float(out[0]), float(out[1])
+    assert e_series <= 2e-7, e_series
+    assert e_den <= 2e-7, e_den
