@@ -295,8 +295,14 @@ __global__ void __launch_bounds__(4 * kRows, 1) k_fused_query_pair(const __grid_
     for (int i = 0; i < KH; ++i) {
       lobe_activate<true>(rh[4 * i], rh[4 * i + 1], rh[4 * i + 2], rh[4 * i + 3], a.mix.kappa_softplus, lam[i],
                           kap[i], mu[i]);
-      nrm[i] = vmf_norm<true>(kap[i]);
-      if (cosine) lobe_cosine<true>(mb, nb, lam[i], kap[i], mu[i], nrm[i]);
+      // below M_EPSILON the lobe is uniform: kappa 0 (e^{0} and 1/4pi, no per-lobe branch in the pdf
+      // or the sampler) and the branch-free normaliser
+      const float kz = kap[i] < NMG_EPS ? 0.f : kap[i];
+      nrm[i] = vmf_norm_sel(kz);
+      if (cosine)
+        lobe_cosine<true>(mb, nb, lam[i], kap[i], mu[i], nrm[i]);  // the product's kappa: 0 or >= 1e-3
+      else
+        kap[i] = kz;
       part += lam[i];
     }
     mine[0] = part;
@@ -385,15 +391,14 @@ __global__ void __launch_bounds__(4 * kRows, 1) k_fused_query_pair(const __grid_
         ks = other[3];
         ms = f3{other[4], other[5], other[6]};
       }
-      d = vmf_sample_dir<true>(ks, ms, u.z, u.w);  // the same inputs in both halves
+      d = vmf_sample_lean(ks, ms, u.z, u.w);  // the same inputs in both halves
     }
     // pdf at d (distribution.h:113-119), this half's lobes
     float pd = 0.f;
 #pragma unroll
     for (int i = 0; i < KH; ++i) {
       const float c = dot3(d, mu[i]);
-      const float v = kap[i] < NMG_EPS ? NMG_INV_4PI : __expf(kap[i] * fminf(0.f, c - 1.f)) * nrm[i];
-      pd += lam[i] * v;
+      pd += lam[i] * (__expf(kap[i] * fminf(0.f, c - 1.f)) * nrm[i]);
     }
     mine[7] = pd;
     ok = bar_red_and(1 + p, 2 * kRows, ok);
