@@ -467,6 +467,7 @@ template <int K> NMG_D int mix_select(const Mix<K>& m, float u) {
 }
 
 template <bool FAST> NMG_D f3 vmf_sample_dir(float k, f3 mu, float u0, float u1);
+NMG_D f3 vmf_sample_lean(float k, f3 mu, float u0, float u1);
 
 // raytracing.h:35-49 Frame(mu) applied to a direction in the lobe's local
 // frame: T = normalize(mu x e), e the branchless axis pick
@@ -495,6 +496,8 @@ NMG_D f3 mix_sample_lobe(const Mix<K>& m, int sel, float u0, float u1) {
       k = m.kap[i];
       mu = m.mu[i];
     }
+  // FAST: the one-logarithm sampler (kappa below M_EPSILON is the uniform lobe, kappa 0 there)
+  if constexpr (FAST) return vmf_sample_lean(k < NMG_EPS ? 0.f : k, mu, u0, u1);
   return vmf_sample_dir<FAST>(k, mu, u0, u1);
 }
 
