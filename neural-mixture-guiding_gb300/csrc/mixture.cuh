@@ -549,11 +549,14 @@ NMG_D float mix_pdf(const Mix<K>& m, f3 wi) {
 }
 
 // ---------------------------------------------------------------------------
-// The mixture-only kernels' form (raw outputs in memory, no cosine lobe,
-// hardware exponentials and divides, table sin/cos of the lobe angles):
-// only what selection, sampling and the pdf need, with the concentration-
-// dependent branches of the general form evaluated branch-free. The lobe
-// selection is the general form's, operation for operation.
+// The lean form (hardware exponentials and divides): only what selection,
+// sampling and the pdf need, with the concentration-dependent branches of
+// the general form evaluated branch-free. MixLean and its activation serve
+// the mixture-only kernels (raw outputs in memory, no cosine lobe, table
+// sin/cos of the lobe angles); the branch-free normaliser and the
+// one-logarithm sampler also serve the network kernels' mixtures (the
+// 16-lobe query, the sampler of the 8-lobe query, the training loss). The
+// lobe selection is the general form's, operation for operation.
 
 // B(x) = x / (1 - e^{-x}) for 0 <= x < 0.5 from its series
 // 1 + x/2 + x^2/12 - x^4/720 + x^6/30240 (the Bernoulli numbers; the first
