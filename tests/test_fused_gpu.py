@@ -384,3 +384,30 @@ def test_pair_tiling_matches_one_thread_per_query(nmg, synth, preset, K):
         assert float((out["selection"] - ref["selection"]).abs().max()) <= 1e-3
     f.check_errors()
     f.close()
+
+
+@pytest.mark.parametrize("tiling", [7, 8, 4])
+def test_16_lobe_direction_stores_any_alignment(nmg, synth, tiling):
+    """The 16-lobe epilogues write a warp's 32 directions as whole-sector float4 rows when the
+    output is 16-byte aligned and every row of the warp is valid, and row by row otherwise. A
+    direction array starting 12 bytes into an allocation (not 16-byte aligned) and a ragged
+    count (a partial last warp) give the same outputs as an aligned array."""
+    import torch
+    n = 40_007
+    f = nmg.GuidingField(nmg.config(1, path=1, n_lobes=16), max_queries=n)
+    perturb(f, 11)
+    f.set_query_tiling(tiling)
+    q = synth.wavefront(n, seed=31)
+    pos, wo, nrm, r, u4 = dev(q["pos"], q["wo"], q["normal"], q["rough"], q["u4"])
+    ref = f.query(pos, wo, nrm, r, u4)
+    back = torch.full((n + 1, 3), float("nan"), device="cuda")
+    out = {"dir": back[1:], "pdf": torch.empty(n, device="cuda"),
+           "lobe": torch.empty(n, device="cuda", dtype=torch.int32)}
+    assert out["dir"].data_ptr() % 16 == 12
+    f.query(pos, wo, nrm, r, u4, outputs=out)
+    torch.cuda.synchronize()
+    assert torch.equal(out["dir"], ref["dir"])
+    assert torch.equal(out["pdf"], ref["pdf"])
+    assert torch.isnan(back[0]).all()  # nothing written before the array
+    f.check_errors()
+    f.close()
