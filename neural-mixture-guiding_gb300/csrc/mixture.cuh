@@ -577,6 +577,14 @@ NMG_D float vmf_norm_sel(float k) {
   return x < 0.5f ? lo : hi;
 }
 
+// 32 bytes of global memory in one load (ld.global.v8.f32, sm_100 and
+// later); p 32-byte aligned. The data must not change during the kernel.
+NMG_D void ld_global_v8(const float* p, float4& a, float4& b) {
+  asm("ld.global.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+
 template <int K> struct MixLean {
   float lam[K];  // activated lambda
   float kap[K];  // concentration; 0 for a lobe below M_EPSILON (uniform, vmf.h:24)
@@ -588,12 +596,22 @@ template <int K> struct MixLean {
 // distribution.h:85-98 for the mixture-only kernels (a kernel using it calls
 // sincospi_tab_fill() first). A lobe below M_EPSILON gets kappa 0: its pdf
 // term e^{0} times 1/4pi is the reference's uniform value exactly.
-template <int K>
+// WIDE: raw is 32-byte aligned in global memory and K is even, and the row
+// comes in as K/2 32-byte loads (ld.global.v8.f32, sm_100 and later): half
+// the load instructions, and half the L1 wavefronts when every lane of a warp
+// reads a different row.
+template <int K, bool WIDE = false>
 NMG_D void mix_activate_lean(MixLean<K>& m, const float* raw, int kappa_softplus) {
+  float4 row[WIDE ? K : 1];
+  if constexpr (WIDE) {
+    static_assert(K % 2 == 0, "32-byte loads take two lobes");
+#pragma unroll
+    for (int j = 0; j < K / 2; ++j) ld_global_v8(raw + 8 * j, row[2 * j], row[2 * j + 1]);
+  }
   m.total = 0.f;
 #pragma unroll
   for (int i = 0; i < K; ++i) {
-    const float4 r = reinterpret_cast<const float4*>(raw)[i];
+    const float4 r = WIDE ? row[WIDE ? i : 0] : reinterpret_cast<const float4*>(raw)[i];
     m.lam[i] = __expf(act_exp_clamp(r.x));
     float k = kappa_softplus ? softplus<true>(r.y) : __expf(act_exp_clamp(r.y));
     k = k < NMG_EPS ? 0.f : k;

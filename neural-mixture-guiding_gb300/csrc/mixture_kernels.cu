@@ -57,12 +57,12 @@ static int resident_grid(Kern kernel, int smem, long n) {
 
 // COS: with the cosine-lobe product (cosn given); without it the query takes
 // the lean form (mix_activate_lean and its selection, sampler and pdf).
-template <int K, bool FAST, bool COS>
+template <int K, bool FAST, bool COS, bool WIDE = false>
 NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int kappa_softplus, float* dir,
                       float* pdf, int* lobe) {
   if constexpr (FAST && !COS) {
     MixLean<K> m;
-    mix_activate_lean<K>(m, row, kappa_softplus);
+    mix_activate_lean<K, WIDE>(m, row, kappa_softplus);
     float k, inv;
     f3 mu;
     const int sel = mix_select_lean<K>(m, u.y, &k, &mu, &inv);
@@ -82,14 +82,15 @@ NMG_D void sample_one(const float* row, float4 u, const float* cosn, long q, int
   if (lobe) lobe[q] = sel;
 }
 
-// Direct 128-bit loads of each query's row and uniforms, one wave of
-// resident blocks (a grid-stride loop). At K <= 8 the bound of 5 blocks per
-// SM lets the lean form keep its lobes in 96 registers without spilling;
-// 2,097,152 queries at K = 8 measured 98 us this way against 115 us with the
-// rows staged in shared memory by per-thread cp.async copies (6 blocks per
-// SM at 80 registers, the staging filling the SM's shared memory) and
-// 108 us with 106 registers and 4 blocks.
-template <int K, bool FAST, bool COS>
+// Direct loads of each query's row and uniforms, one wave of resident blocks
+// (a grid-stride loop). WIDE: 32-byte row loads (rows_32b). At K <= 8 the
+// bound of 5 blocks per SM lets the lean form keep its lobes in 96 registers
+// without spilling. 2,097,152 queries at K = 8: 90 us with 32-byte loads,
+// 98 us with 16-byte loads (the L1 data pipe was then 73% busy with their
+// wavefronts, one line per lane and load), 115 us with the rows staged in
+// shared memory by per-thread cp.async copies (6 blocks per SM at 80
+// registers), 108 us with 106 registers and 4 blocks.
+template <int K, bool FAST, bool COS, bool WIDE = false>
 __global__ void __launch_bounds__(kThreads, K <= 8 ? 5 : 1) k_mixture_sample(const float* __restrict__ raw,
                                                                              int stride,
                                                                              const float* __restrict__ u4,
@@ -101,8 +102,14 @@ __global__ void __launch_bounds__(kThreads, K <= 8 ? 5 : 1) k_mixture_sample(con
   sincospi_tab_fill();
   const long step = long(gridDim.x) * blockDim.x;
   for (long q = long(blockIdx.x) * blockDim.x + threadIdx.x; q < n; q += step)
-    sample_one<K, FAST, COS>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q, kappa_softplus, dir,
-                             pdf, lobe);
+    sample_one<K, FAST, COS, WIDE>(raw + q * stride, reinterpret_cast<const float4*>(u4)[q], cosn, q,
+                                   kappa_softplus, dir, pdf, lobe);
+}
+
+// Whether a row-major raw array can be read with 32-byte loads: rows of a
+// multiple of 8 floats from a 32-byte aligned base.
+static bool rows_32b(const float* raw, int stride) {
+  return stride % 8 == 0 && (reinterpret_cast<uintptr_t>(raw) & 31u) == 0;
 }
 
 template <int K, bool FAST>
@@ -238,11 +245,12 @@ __global__ void __launch_bounds__(kThreads, K <= 8 ? 8 : 1) k_mixture_pdf2(const
 
 // train.cu:69-172 with the lobes split over a lane pair: each lane computes
 // its lobes' activations, vMF values and gradients; q and the total come
-// from the pair's partial sums. Direct loads; 8 blocks per SM at K <= 8
-// (64 registers): 154 us for 2,097,152 queries at K = 8, against 178 us
-// with the rows staged in shared memory by per-thread cp.async copies and
+// from the pair's partial sums. Direct loads (WIDE: 32-byte loads of the
+// half row, rows_32b); 8 blocks per SM at K <= 8 (64 registers). 2,097,152
+// queries at K = 8: 152 us with 32-byte loads, 154 us with 16-byte loads,
+// 178 us with the rows staged in shared memory by per-thread cp.async copies,
 // 166 us at the 89 registers the compiler picks unbounded.
-template <int K, bool SEL>
+template <int K, bool SEL, bool WIDE = false>
 __global__ void __launch_bounds__(kThreads, K <= 8 ? 8 : 1) k_mixture_loss_grad2(const float* __restrict__ raw,
                                                                                int stride,
                                                                                const float* __restrict__ rec,
@@ -268,9 +276,14 @@ __global__ void __launch_bounds__(kThreads, K <= 8 ? 8 : 1) k_mixture_loss_grad2
     const f3 wi{swt * cwp, swt * swp, cwt};
     float lam[KH], kap[KH], dkap[KH], vmf[KH], cc[KH], dta[KH], dpa[KH], sgt[KH], sgp[KH];
     float lt = 0.f, nt = 0.f;
+    float4 xw[WIDE ? KH : 1];  // WIDE: the half row in 32-byte loads (see mix_activate_lean)
+    if constexpr (WIDE) {
+#pragma unroll
+      for (int j = 0; j < KH / 2; ++j) ld_global_v8(row + 8 * j, xw[2 * j], xw[2 * j + 1]);
+    }
 #pragma unroll
     for (int i = 0; i < KH; ++i) {
-      const float4 x = reinterpret_cast<const float4*>(row)[i];
+      const float4 x = WIDE ? xw[WIDE ? i : 0] : reinterpret_cast<const float4*>(row)[i];
       lam[i] = xexp<FAST>(act_exp_clamp(x.x));
       if (o.kappa_softplus) {
         kap[i] = softplus<FAST>(x.y);
@@ -350,6 +363,10 @@ static nmg_status launch_sample(const nmg_mixture_opts* o, const float* raw, con
     const int grid = resident_grid(k_mixture_sample<K, kMixFast, true>, 0, n);
     k_mixture_sample<K, kMixFast, true><<<grid, kThreads, 0, st>>>(raw, o->stride, u4, cosn, n, o->kappa_softplus,
                                                                    dir, pdf, lobe);
+  } else if (K % 2 == 0 && rows_32b(raw, o->stride)) {
+    const int grid = resident_grid(k_mixture_sample<K, kMixFast, false, K % 2 == 0>, 0, n);
+    k_mixture_sample<K, kMixFast, false, K % 2 == 0><<<grid, kThreads, 0, st>>>(raw, o->stride, u4, nullptr, n,
+                                                                                o->kappa_softplus, dir, pdf, lobe);
   } else {
     const int grid = resident_grid(k_mixture_sample<K, kMixFast, false>, 0, n);
     k_mixture_sample<K, kMixFast, false><<<grid, kThreads, 0, st>>>(raw, o->stride, u4, nullptr, n,
@@ -367,6 +384,7 @@ static nmg_status launch_pdf(const nmg_mixture_opts* o, const float* raw, const 
       k_mixture_pdf2<K, kMixFast, true><<<grid, kThreads, 0, st>>>(raw, o->stride, wi, cosn, n, o->kappa_softplus,
                                                                    pdf);
     } else {
+      // (the 32-byte row loads of the sampler and the loss measured 71.7 against 69.6 us here)
       const int grid = resident_grid(k_mixture_pdf2<K, kMixFast, false>, 0, 2L * n);
       k_mixture_pdf2<K, kMixFast, false><<<grid, kThreads, 0, st>>>(raw, o->stride, wi, nullptr, n,
                                                                     o->kappa_softplus, pdf);
@@ -389,6 +407,11 @@ static nmg_status launch_loss(const nmg_mixture_opts* o, const float* raw, const
       blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, true>, 0, 2L * n));
       k_mixture_loss_grad2<K, true><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
                                                                  loss, loss_sum ? partials : nullptr);
+    } else if ((K / 2) % 2 == 0 && rows_32b(raw, o->stride)) {
+      constexpr bool W = (K / 2) % 2 == 0;
+      blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, false, W>, 0, 2L * n));
+      k_mixture_loss_grad2<K, false, W><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo,
+                                                                     grad, loss, loss_sum ? partials : nullptr);
     } else {
       blocks = std::min(blocks, resident_grid(k_mixture_loss_grad2<K, false>, 0, 2L * n));
       k_mixture_loss_grad2<K, false><<<blocks, kThreads, 0, st>>>(raw, o->stride, rec, rstride, n, scale, mo, grad,
