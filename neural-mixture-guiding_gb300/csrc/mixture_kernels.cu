@@ -1,9 +1,11 @@
 // mixture_kernels.cu -- FP32 mixture kernels on raw network outputs and their
 // C-ABI entry points (nmg_mixture_*).
 //
-// One thread per query, lobes in registers, grid-stride loops over a grid of
-// a few waves of the 152 SMs. Each query reads its raw row with 128-bit
-// loads (K float4) and its uniforms as one float4.
+// Sampling takes one thread per query, the pdf and the loss a lane pair per
+// query (half the lobes each); lobes in registers; grid-stride loops over one
+// wave of resident blocks. Each query reads its raw row directly: 32-byte
+// loads (two lobes) where the rows are 32-byte aligned for sampling and the
+// loss, else 16-byte loads (one lobe); its uniforms as one float4.
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
