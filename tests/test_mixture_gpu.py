@@ -207,3 +207,23 @@ def test_lobe_counts_and_ragged_sizes(nmg, oracle, synth, K):
         err = np.abs(g.cpu().numpy()[:, :nout] - g64[:, :nout]).max(axis=1)
         assert np.all(err <= 1e-3 * np.maximum(1.0, np.abs(g64[:, :nout]).max(axis=1))), err.max()
         assert abs(float(tot.cpu()[0]) - t64) <= 1e-5 * abs(t64) + 1e-6
+
+
+def test_row_alignment_paths_agree(nmg, synth):
+    """Raw rows 32-byte aligned (sampling and loss read them with 32-byte loads) and rows starting 16
+    bytes into an allocation (16-byte loads): the same directions, pdfs, lobes and gradients."""
+    import torch
+    raw, u4, rec = synth.mixture_batch(10_001, 8, seed=77)
+    r, u, rc = to_dev(raw, u4, rec)
+    flat = torch.empty(r.numel() + 4, device="cuda")
+    r_off = flat[4:].view_as(r)
+    r_off.copy_(r)
+    assert r.data_ptr() % 32 == 0 and r_off.data_ptr() % 32 == 16
+    d0, p0, l0 = nmg.mixture_sample(r, u, 8)
+    d1, p1, l1 = nmg.mixture_sample(r_off, u, 8)
+    assert torch.equal(d0, d1) and torch.equal(p0, p1) and torch.equal(l0, l1)
+    g0, s0, t0 = nmg.mixture_loss_grad(r, rc, 8)
+    g1, s1, t1 = nmg.mixture_loss_grad(r_off, rc, 8)
+    assert torch.equal(g0, g1) and torch.equal(s0, s1)
+    # the FP64 loss sum may add the same per-query losses in another block order
+    assert abs(float(t0.cpu()[0]) - float(t1.cpu()[0])) <= 1e-12 * abs(float(t0.cpu()[0]))
